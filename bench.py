@@ -1,0 +1,394 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 state-vector engine on the 30-qubit random circuit.
+
+Workload (the headline configuration): 30 qubits, depth 20; each layer applies
+U3(theta, phi, lambda) to every qubit with angles uniform in [0, 2pi)
+(numpy default_rng(10), shape (20, 30, 3)), then CX on a random perfect
+matching of the qubits (default_rng(11).permutation(30) per layer: pairs
+(p[2k], p[2k+1]), control first).  complex64 by default (--dtype c128 for
+complex128).  Inputs are synthetic; the state (8 GiB in complex64) is far
+larger than the 129 MB L2, so no L2 flush is needed between steps.
+
+A step = reset the resident state to |0...0> and run the 900-gate circuit
+through the runtime plugin API (gates are queued, fused into shared-memory
+stages and launched at synchronize).  `value` = algorithmic bytes of the
+gate passes executed (one read + one write of every touched amplitude) per
+second of device time.  `e2e` = the same bytes per second of a step that
+also brings the circuit's outputs to the host through the plugin API: the
+full probability vector and 1e7 samples drawn from pre-drawn uniforms.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`--impl reference` times the reference's CPU algorithm (the oracle's C port
+of the reference CPU runtime, all host threads) on the same workload and
+metric, on a bounded sample of the circuit's gates per step.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = '30q gate-pass GB/s'
+
+
+def circuit(n, depth, seed_angles=10, seed_perm=11):
+    """[(name, args, target, controls)] of the random U3 + CX circuit."""
+    ang = np.random.default_rng(seed_angles).uniform(0, 2 * math.pi, (depth, n, 3))
+    prng = np.random.default_rng(seed_perm)
+    ops = []
+    for layer in range(depth):
+        ops += [('U', tuple(float(a) for a in ang[layer, q]), q, ()) for q in range(n)]
+        p = prng.permutation(n)
+        ops += [('X', (), int(p[2 * k + 1]), (int(p[2 * k]),)) for k in range(n // 2)]
+    return ops
+
+
+def gate_pass_bytes(n, ops, cs):
+    """Unfused algorithmic bytes: each gate reads and writes the amplitudes it
+    touches (2^(n - #controls))."""
+    return sum(2 * (1 << (n - len(c))) * cs for _, _, _, c in ops)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(',')]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        return {'sm_mhz': statistics.median(sm) if sm else None,
+                'sm_max_mhz': max(smax) if smax else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return float(json.load(f)['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def stage_traffic_per_launch(n, cs):
+    """DRAM bytes per fused-stage launch from the committed ncu summary
+    (profiles/stage_traffic.json: bytes per amplitude measured on a smaller
+    state, scaled to 2^n amplitudes), or None."""
+    try:
+        with open(os.path.join(ROOT, 'profiles', 'stage_traffic.json')) as f:
+            d = json.load(f)
+        key = 'c64' if cs == 8 else 'c128'
+        return float(d[key]['dram_bytes_per_amp']) * (1 << n)
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ CPU legs
+
+def cpu_port_gate_rate(n, ops, cs, budget_s):
+    """Times the oracle's C port of the reference CPU runtime on the first
+    gates of the circuit until `budget_s` seconds are spent.  Returns
+    (GB/s, gates timed, seconds, threads)."""
+    from oracle import cpu_port, statevec as sv
+    st = cpu_port.State(n, np.complex64 if cs == 8 else np.complex128)
+    mats = {}
+    done, nbytes = 0, 0
+    t0 = time.perf_counter()
+    for name, args, target, ctrls in ops:
+        key = (name, args)
+        if key not in mats:
+            mats[key] = sv.gate_matrix(name, args)
+        st.apply(mats[key], target, ctrls)
+        done += 1
+        nbytes += 2 * (1 << (n - len(ctrls))) * cs
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return nbytes / dt / 1e9, done, dt, cpu_port.num_threads()
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    n, cs = args.qubits, 16 if args.dtype == 'c128' else 8
+    ops = circuit(n, args.depth)
+    from oracle import cpu_port, statevec as sv
+    st = cpu_port.State(n, np.complex64 if cs == 8 else np.complex128)
+    sample = ops[:args.ref_gates]
+    mats = [sv.gate_matrix(nm, a) for nm, a, _, _ in sample]
+    step_bytes = gate_pass_bytes(n, sample, cs)
+    for _ in range(args.warmup):
+        for m, (_, _, t, c) in zip(mats, sample):
+            st.apply(m, t, c)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for m, (_, _, t, c) in zip(mats, sample):
+            st.apply(m, t, c)
+    dt = time.perf_counter() - t0
+    value = step_bytes * args.steps / dt / 1e9
+    sample_desc = ('first %d gates of the circuit per step on a 2^%d %s state in host memory'
+                   % (len(sample), n, args.dtype))
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'GB/s',
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': dt / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': args.dtype, 'data': 'synthetic',
+        'config': config_block(args, None),
+        'cpu_baseline': {'value': value, 'unit': 'GB/s', 'cores': cpu_port.num_threads(),
+                         'kind': 'port', 'sample': sample_desc},
+        'e2e': {'value': value, 'unit': 'GB/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_block(args, extra):
+    cfg = {'workload': 'random U3+CX circuit, %d qubits, depth %d, %s (layers: U3 on every '
+                       'qubit, CX on a seeded random matching)' % (args.qubits, args.depth,
+                                                                    args.dtype),
+           'qubits': args.qubits, 'depth': args.depth, 'gates': args.qubits * args.depth +
+           (args.qubits // 2) * args.depth,
+           'l2': 'state larger than L2 (no flush needed)', 'parallelism': 'replicas'}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ------------------------------------------------------------------ GPU leg
+
+def run_gb300(args):
+    import torch
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('gloo')
+    torch.cuda.set_device(local)
+
+    from qgate_gb300 import _native as nat
+    from qgate_gb300 import gb300runtime as rt
+    from qgate_gb300.circuit import gate_type, Lane, abs2
+
+    rt.set_preference(device_ids=[local])
+    n, cs = args.qubits, 16 if args.dtype == 'c128' else 8
+    dtype = np.float64 if args.dtype == 'c128' else np.float32
+    ops = circuit(n, args.depth)
+    gts = [(gate_type(nm, *a), t, list(c)) for nm, a, t, c in ops]
+    nat.set_fusion(args.tile)
+
+    qs = rt.create_qubit_states(dtype)
+    proc = qs.processor
+    proc.initialize_qubit_states(qs, n)
+
+    def step():
+        proc.reset_qubit_states(qs)
+        for gt, t, c in gts:
+            if c:
+                proc.apply_controlled_gate(gt, False, qs, c, t)
+            else:
+                proc.apply_gate(gt, False, qs, t)
+        proc.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    stream = torch.cuda.ExternalStream(nat.stream_handle())
+    nat.gate_stats(reset=True)
+    nat.timing_all(reset=True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    nat.timing_enable(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    nat.timing_enable(False)
+    clocks = sampler.stop()
+    dev_ms = e0.elapsed_time(e1)
+    stats = nat.gate_stats(reset=True)
+    timing = nat.timing_all(reset=True)
+    init_bytes = (1 << n) * cs * args.steps
+    moved = stats['bytes'] + init_bytes
+    t_max = dev_ms
+    if world > 1:
+        t = torch.tensor([dev_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t[0])
+    value = moved * world / (t_max / 1e3) / 1e9
+    launches = sum(v[0] for v in timing.values())
+
+    # roofline of the dominant kernel class
+    dom = max(timing.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_ms) = dom
+    peak, peak_kind = measured_peak_hbm()
+    if dom_name == 'stage':
+        alg = 2 * (1 << n) * cs
+        traffic = stage_traffic_per_launch(n, cs)
+    else:
+        alg = stats['bytes'] / max(1, stats['passes'])
+        traffic = None
+    achieved = alg / (dom_ms / dom_launches / 1e3) / 1e9 if dom_launches else 0.
+    roofline = {'kernel': {'stage': 'k_stage (fused shared-memory stage)',
+                           'gate': 'k_pairs (single gate)'}.get(dom_name, dom_name),
+                'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                'frac': achieved / peak, 'peak_source': peak_kind,
+                'traffic': traffic, 'algorithmic_bytes_per_launch': alg,
+                'launches': dom_launches, 'avg_launch_ms': dom_ms / max(1, dom_launches)}
+
+    # end to end through the plugin API with host buffers
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        gbs, done, dt, thr = cpu_port_gate_rate(n, ops, cs, args.cpu_seconds)
+        cpu = {'value': gbs, 'unit': 'GB/s', 'cores': thr, 'kind': 'port',
+               'sample': 'first %d gates of the circuit on a 2^%d %s state in host memory, '
+                         '%.1f s' % (done, n, args.dtype, dt)}
+
+    if rank == 0:
+        per_step_passes = stats['passes'] / args.steps
+        line = {
+            'metric': METRIC, 'value': value, 'unit': 'GB/s', 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_max / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': args.dtype, 'data': 'synthetic',
+            'config': config_block(args, {
+                'fusion_tile_lanes': args.tile, 'passes_per_step': per_step_passes,
+                'gates_per_step': stats['gates'] / args.steps,
+                'gate_pass_bytes_per_step': stats['bytes'] / args.steps,
+                'unfused_gate_pass_bytes_per_step': gate_pass_bytes(n, ops, cs),
+                'circuit_ms': t_max / args.steps,
+                'gates_per_s': stats['gates'] / args.steps / (t_max / args.steps / 1e3)}),
+            'roofline': roofline,
+            'cpu_baseline': cpu,
+            'e2e': e2e,
+            'gpu_launches': launches,
+            'kernel_ms': {k: v[1] for k, v in timing.items() if v[0]},
+            'clocks': clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2):
+    """Same metric through the plugin API with host buffers: circuit, full
+    probability vector to host, pool + 1e7 samples from host uniforms."""
+    getter = rt.create_qubits_states_getter(dtype)
+    u = np.random.default_rng(12).random(args.samples)
+    probs = np.empty(1 << n, dtype)
+
+    def lane_trans():
+        return [(qs, [Lane(l, l) for l in range(n)])]
+
+    def e2e_step():
+        step()
+        getter.get_states(probs, 0, abs2, lane_trans(), [], 1 << n, 0, 1)
+        pool = getter.create_sampling_pool(list(range(n)), n, 0, lane_trans(), [])
+        obs = pool.sample(args.samples, u)
+        pool.delete()
+        return obs
+
+    e2e_step()
+    nat.gate_stats(reset=True)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    dt = time.perf_counter() - t0
+    stats = nat.gate_stats(reset=True)
+    moved = stats['bytes'] + (1 << n) * cs * args.e2e_steps
+    return {'value': moved / dt / 1e9, 'unit': 'GB/s',
+            'h2d_bytes_per_step': args.samples * 8 + len(ops) * 64,
+            'd2h_bytes_per_step': (1 << n) * (cs // 2) + args.samples * 8,
+            'steps': args.e2e_steps, 'ms_per_step': dt / args.e2e_steps * 1e3,
+            'outputs': 'probability vector (2^%d %s) + %d samples' % (
+                n, 'float32' if cs == 8 else 'float64', args.samples)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--qubits', type=int, default=30)
+    ap.add_argument('--depth', type=int, default=20)
+    ap.add_argument('--dtype', default='c64', choices=['c64', 'c128'])
+    ap.add_argument('--tile', type=int, default=0, help='fusion tile lanes (0 = default, 1 = off)')
+    ap.add_argument('--samples', type=int, default=10_000_000)
+    ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--ref-gates', type=int, default=12)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == 'gb300':
+        print('note: fewer than 3 warm-up steps', file=sys.stderr)
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == '__main__':
+    main()

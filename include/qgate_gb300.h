@@ -1,0 +1,222 @@
+/*
+ * qgate_gb300 — C ABI of the GB300 (sm_103a) state-vector engine.
+ *
+ * Every entry point returns an int status (QG_OK on success) and never throws
+ * or aborts across the boundary; the message of the last failure on the
+ * calling thread is returned by qg_last_error().  Handles are opaque 64-bit
+ * values owned by the caller and released with the matching *_delete call.
+ *
+ * The set of entry points mirrors the reference's CPython glue for its native
+ * runtimes (qgate/simulator/src/glue.cpp:605-631 and
+ * qgate/simulator/src/cudaext.cpp:127-136), with Python objects replaced by
+ * plain pointers and sizes.  Each declaration names the reference entry point
+ * it replaces.  Entries marked "extension" have no counterpart in the
+ * reference and implement capabilities the reference lacks.
+ *
+ * Precision codes follow the reference's `enum Precision`
+ * (qgate/simulator/src/Types.h:49-53): QG_PREC_FP64 = complex128 states,
+ * QG_PREC_FP32 = complex64 states.  Math ops follow `enum MathOp`
+ * (qgate/simulator/src/Types.h:55-58).
+ *
+ * Gate matrices are 2x2 complex128, row-major, passed as 8 doubles
+ * {re00, im00, re01, im01, re10, im10, re11, im11} — the layout of the
+ * reference's Matrix2x2C64 (qgate/simulator/src/Types.h:22-46).
+ */
+#ifndef QGATE_GB300_H
+#define QGATE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef uint64_t qg_handle;
+
+enum {
+    QG_OK = 0,
+    QG_ERR_VALUE = 1,    /* invalid argument (reference raises ValueError) */
+    QG_ERR_RUNTIME = 2,  /* invalid state / semantic error (RuntimeError) */
+    QG_ERR_CUDA = 3,     /* CUDA runtime failure */
+    QG_ERR_NOMEM = 4,    /* "Out of device memory." */
+    QG_ERR_TIMEOUT = 5   /* a bounded device-side wait gave up */
+};
+
+enum { QG_PREC_FP64 = 1, QG_PREC_FP32 = 2 };
+enum { QG_MATHOP_NULL = 0, QG_MATHOP_PROB = 1 };
+
+/* Message of the last failure on this thread ("" if none). */
+const char *qg_last_error(void);
+
+/* ---- device / module --------------------------------------------------- */
+
+/* Replaces cudaext.devices_initialize (qgate/simulator/src/cudaext.cpp:32-58).
+ * One GPU only: device_id selects it (-1 = current device).  memory_limit
+ * caps the arena in bytes (-1 = no cap beyond device memory). */
+int qg_devices_initialize(int device_id, int64_t memory_limit);
+
+/* Replaces cudaext.devices_clear / module_finalize
+ * (qgate/simulator/src/cudaext.cpp:23-29, 60-67).  Frees the arena cache. */
+int qg_devices_clear(void);
+
+/* Bytes currently handed out by / cached in the device arena (diagnostics;
+ * the reference reports leaks at finalize,
+ * qgate/simulator/src/MultiDeviceMemoryStore.cpp:33-43). */
+int qg_arena_stats(int64_t *in_use, int64_t *cached);
+
+/* ---- qubit states (qgate/simulator/src/Interfaces.h:7-20) -------------- */
+
+/* Replaces cudaext.qubit_states_new (qgate/simulator/src/cudaext.cpp:70-87). */
+int qg_qubit_states_new(int prec, qg_handle *out);
+/* Replaces glue.qubit_states_delete (qgate/simulator/src/glue.cpp:193-205). */
+int qg_qubit_states_delete(qg_handle qstates);
+/* Replaces glue.qubit_states_deallocate (qgate/simulator/src/glue.cpp:180-190). */
+int qg_qubit_states_deallocate(qg_handle qstates);
+/* Replaces glue.qubit_states_get_n_lanes (qgate/simulator/src/glue.cpp:237-246). */
+int qg_qubit_states_get_n_lanes(qg_handle qstates, int *n_lanes);
+
+/* ---- qubit processor (qgate/simulator/src/Interfaces.h:22-52) ---------- */
+
+/* Replaces cudaext.qubit_processor_new (qgate/simulator/src/cudaext.cpp:90-106). */
+int qg_qubit_processor_new(int prec, qg_handle *out);
+/* Replaces glue.qubit_processor_delete (qgate/simulator/src/glue.cpp:208-219). */
+int qg_qubit_processor_delete(qg_handle proc);
+/* Replaces glue.qubit_processor_synchronize (qgate/simulator/src/glue.cpp:251-260). */
+int qg_qubit_processor_synchronize(qg_handle proc);
+/* Replaces glue.qubit_processor_reset (qgate/simulator/src/glue.cpp:263-272). */
+int qg_qubit_processor_reset(qg_handle proc);
+/* Replaces glue.qubit_processor_initialize_qubit_states (qgate/simulator/src/glue.cpp:275-286). */
+int qg_qubit_processor_initialize_qubit_states(qg_handle proc, qg_handle qstates, int n_lanes);
+/* Replaces glue.qubit_processor_reset_qubit_states (qgate/simulator/src/glue.cpp:289-299). */
+int qg_qubit_processor_reset_qubit_states(qg_handle proc, qg_handle qstates);
+/* Replaces glue.qubit_processor_calc_probability (qgate/simulator/src/glue.cpp:302-311).
+ * Pr(lane == 0), accumulated in FP64 for both precisions. */
+int qg_qubit_processor_calc_probability(qg_handle proc, qg_handle qstates, int local_lane,
+                                        double *prob);
+/* Replaces glue.qubit_processor_join (qgate/simulator/src/glue.cpp:314-334).  Kronecker product
+ * of the listed states (the last one in the lowest lanes), followed by
+ * n_new_lanes |0> lanes in the highest positions. */
+int qg_qubit_processor_join(qg_handle proc, qg_handle qstates, const qg_handle *qstates_list,
+                            int n_list, int n_new_lanes);
+/* Replaces glue.qubit_processor_decohere (qgate/simulator/src/glue.cpp:337-348). */
+int qg_qubit_processor_decohere(qg_handle proc, int value, double prob, qg_handle qstates,
+                                int local_lane);
+/* Replaces glue.qubit_processor_decohere_and_separate (qgate/simulator/src/glue.cpp:351-365). */
+int qg_qubit_processor_decohere_and_separate(qg_handle proc, int value, double prob,
+                                             qg_handle qstates0, qg_handle qstates1,
+                                             qg_handle qstates, int local_lane);
+/* Replaces glue.qubit_processor_apply_reset (qgate/simulator/src/glue.cpp:368-379). */
+int qg_qubit_processor_apply_reset(qg_handle proc, qg_handle qstates, int local_lane);
+/* Replaces glue.qubit_processor_apply_gate (qgate/simulator/src/glue.cpp:383-405); the matrix is
+ * built by the caller (qg_gate_matrix) instead of a Python factory object. */
+int qg_qubit_processor_apply_gate(qg_handle proc, const double *mat, qg_handle qstates,
+                                  int local_lane);
+/* Replaces glue.qubit_processor_apply_controlled_gate (qgate/simulator/src/glue.cpp:409-432). */
+int qg_qubit_processor_apply_controlled_gate(qg_handle proc, const double *mat,
+                                             qg_handle qstates, const int *local_control_lanes,
+                                             int n_controls, int local_target_lane);
+
+/* Extension: dense 2^k x 2^k complex128 matrix (row-major, interleaved re/im)
+ * on k target lanes (targets[0] = least significant matrix bit), optionally
+ * controlled.  k <= 6.  Replaces the reference's expansions of multi-qubit
+ * gates into CX chains (qgate/model/expand.py:14-16). */
+int qg_qubit_processor_apply_multi(qg_handle proc, const double *mat, qg_handle qstates,
+                                   const int *targets, int n_targets,
+                                   const int *local_control_lanes, int n_controls);
+
+/* Extension: <psi|P|psi> for one Pauli string, FP64 accumulation.
+ * x_mask = lanes carrying X or Y, z_mask = lanes carrying Z or Y.  Replaces
+ * the reference's diagonalise -> Prob -> undo chain
+ * (qgate/model/pauli_gates_diagonalizer.py:96-135, qgate/model/expand.py:66-77):
+ * Pr(+1) of that chain equals (1 + <P>) / 2. */
+int qg_qubit_processor_calc_pauli_expectation(qg_handle proc, qg_handle qstates,
+                                              uint64_t x_mask, uint64_t z_mask, double *out);
+
+/* Extension: sum |psi|^2 in FP64. */
+int qg_qubit_processor_calc_norm(qg_handle proc, qg_handle qstates, double *out);
+
+/* Extension: gate fusion control.  max_tile_lanes = lanes staged per tile in
+ * shared memory by the fused stage kernel (0 = autotuned default, 1 = off:
+ * every gate is its own pass).  Pending gates are flushed at every
+ * observation, join, measure or synchronize. */
+int qg_set_fusion(int max_tile_lanes);
+/* Extension: counters of the gate path since the last reset
+ * {gates, passes, bytes_moved}. */
+int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset);
+
+/* Extension: per-kernel-class launch timing with CUDA events recorded on the
+ * engine's stream around each launch (classes: stage, gate, multi, init,
+ * prob, pauli, measure, join, gather, marginal, scan, search). */
+int qg_timing_enable(int on);
+int qg_timing_read(const char *kernel_class, int64_t *launches, double *total_ms, int reset);
+/* Extension: device facts {SMs, max opt-in shared memory per block, L2 bytes,
+ * pageable memory access, ... uses host page tables, concurrent managed
+ * access, CC major, CC minor, SM clock kHz, memory clock kHz, free bytes,
+ * total bytes} (first n entries). */
+int qg_device_info(int64_t *info, int n);
+/* Extension: the engine's CUDA stream (cudaStream_t) for interop. */
+int qg_get_stream(uint64_t *stream);
+
+/* Extension: copy raw amplitudes between a states object and host memory
+ * (2^n_lanes complex values in the state's precision). */
+int qg_qubit_states_get_raw(qg_handle qstates, void *host, int64_t n);
+int qg_qubit_states_set_raw(qg_handle qstates, const void *host, int64_t n);
+
+/* ---- gate matrices (qgate/simulator/src/GateMatrix.cpp:13-158) --------- */
+
+/* Replaces glue.register_matrix_factory + the MatFactory call in
+ * glue.qubit_processor_apply_gate (qgate/simulator/src/glue.cpp:93-134, 389-395).
+ * name: U, U2, U1, ID, X, Y, Z, H, S, T, RX, RY, RZ, ExpiI, ExpiZ, SH. */
+int qg_gate_matrix(const char *name, const double *args, int n_args, int adjoint, double *mat);
+
+/* ---- states getter (qgate/simulator/src/Interfaces.h:55-72) ------------ */
+
+/* Replaces cudaext.qubits_states_getter_new (qgate/simulator/src/cudaext.cpp:109-125). */
+int qg_qubits_states_getter_new(int prec, qg_handle *out);
+/* Replaces glue.qubits_states_getter_delete (qgate/simulator/src/glue.cpp:222-233). */
+int qg_qubits_states_getter_delete(qg_handle getter);
+
+/* Replaces glue.qubits_states_getter_get_states (qgate/simulator/src/glue.cpp:448-506).
+ * lane_tables holds, for each of the n_qstates states, its
+ * local-lane -> external-lane table (lane_counts[i] entries each,
+ * concatenated).  values is a host array of n_states elements of
+ * complex (mathop NULL) or real (mathop PROB) in the getter's precision,
+ * written from values[array_offset].  Element i is taken at external index
+ * start + step * i (step may be negative). */
+int qg_qubits_states_getter_get_states(qg_handle getter, void *values, int64_t array_offset,
+                                       int mathop, const int *lane_tables,
+                                       const int *lane_counts, const qg_handle *qstates_list,
+                                       int n_qstates, uint64_t empty_lane_mask, int n_qregs,
+                                       int64_t n_states, int64_t start, int64_t step);
+
+/* Replaces glue.qubits_states_getter_prepare_prob_array (qgate/simulator/src/glue.cpp:509-536).
+ * Writes 2^n_lanes marginal probabilities (hidden lanes summed out) to the
+ * host array prob in the getter's precision; accumulation is FP64. */
+int qg_qubits_states_getter_prepare_prob_array(qg_handle getter, void *prob,
+                                               const int *lane_tables, const int *lane_counts,
+                                               const qg_handle *qstates_list, int n_qstates,
+                                               int n_lanes, int n_hidden_lanes);
+
+/* Replaces glue.qubits_states_getter_create_sampling_pool (qgate/simulator/src/glue.cpp:539-559).
+ * The pool keeps an FP64 cumulative distribution in device memory. */
+int qg_qubits_states_getter_create_sampling_pool(qg_handle getter, const int *lane_tables,
+                                                 const int *lane_counts,
+                                                 const qg_handle *qstates_list, int n_qstates,
+                                                 int n_lanes, int n_hidden_lanes,
+                                                 const int *empty_lanes, int n_empty_lanes,
+                                                 qg_handle *out);
+
+/* ---- sampling pool (qgate/simulator/src/Interfaces.h:75-80) ------------ */
+
+/* Replaces glue.sampling_pool_sample (qgate/simulator/src/glue.cpp:562-589): obs[i] =
+ * upper_bound(cdf, randnum[i]) with empty-lane zero bits inserted. */
+int qg_sampling_pool_sample(qg_handle pool, int64_t *obs, int64_t n_samples,
+                            const double *randnum);
+/* Replaces glue.sampling_pool_delete (qgate/simulator/src/glue.cpp:592-603). */
+int qg_sampling_pool_delete(qg_handle pool);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QGATE_GB300_H */

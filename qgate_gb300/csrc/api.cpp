@@ -1,0 +1,1222 @@
+// extern "C" boundary of the GB300 state-vector engine: device context,
+// caching arena, states / processor / getter / pool objects, the gate queue
+// with its fusion planner, and the host side of every entry point declared
+// in include/qgate_gb300.h.
+//
+// One GPU, one non-blocking stream: every launch is stream-ordered, so a
+// buffer returned to the arena can be handed out again without waiting.
+// The host synchronises only where a value must come back (probabilities,
+// expectations, gathers, sampling), as the reference's CUDA runtime does
+// (qgate/simulator/src/CUDAQubitProcessor.cpp:40-50,
+// qgate/simulator/src/DeviceSum.h:16-23).
+#include "qg_internal.h"
+#include "../../include/qgate_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <set>
+#include <unordered_map>
+#include <unordered_set>
+
+namespace qg {
+
+static thread_local std::string t_last_error;
+
+void fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    throw Error{code, std::string(buf)};
+}
+
+void cuda_check(cudaError_t err, const char *what) {
+    if (err == cudaSuccess) return;
+    if (err == cudaErrorMemoryAllocation) fail(QG_ERR_NOMEM, "Out of device memory. (%s)", what);
+    fail(QG_ERR_CUDA, "CUDA error %d (%s) in %s", (int)err, cudaGetErrorString(err), what);
+}
+
+// ------------------------------------------------------------ arena
+
+// Caching allocator with power-of-two size classes, the single-device
+// counterpart of the reference's chunk cache
+// (qgate/simulator/src/MultiDeviceMemoryStore.cpp:164-201).
+struct Arena {
+    std::map<size_t, std::vector<void *>> free_lists;
+    std::unordered_map<void *, size_t> live;
+    size_t in_use = 0, cached = 0;
+    long long limit = -1;
+
+    static size_t size_class(size_t bytes) {
+        size_t c = 256;
+        while (c < bytes) c <<= 1;
+        return c;
+    }
+    void trim() {
+        for (auto &kv : free_lists)
+            for (void *p : kv.second) cudaFree(p);
+        free_lists.clear();
+        cached = 0;
+    }
+    void *alloc(size_t bytes) {
+        size_t cls = size_class(bytes);
+        auto it = free_lists.find(cls);
+        if (it != free_lists.end() && !it->second.empty()) {
+            void *p = it->second.back();
+            it->second.pop_back();
+            cached -= cls;
+            in_use += cls;
+            live[p] = cls;
+            return p;
+        }
+        if (limit >= 0 && (long long)(in_use + cls) > limit)
+            fail(QG_ERR_NOMEM, "Out of device memory. (arena limit %lld bytes, requested %zu)",
+                 limit, cls);
+        if (limit >= 0 && (long long)(in_use + cached + cls) > limit) trim();
+        void *p = nullptr;
+        cudaError_t err = cudaMalloc(&p, cls);
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            trim();
+            err = cudaMalloc(&p, cls);
+            if (err != cudaSuccess) {
+                cudaGetLastError();
+                fail(QG_ERR_NOMEM, "Out of device memory. (requested %zu bytes)", cls);
+            }
+        }
+        in_use += cls;
+        live[p] = cls;
+        return p;
+    }
+    void release(void *p) {
+        if (!p) return;
+        auto it = live.find(p);
+        if (it == live.end()) return;
+        size_t cls = it->second;
+        live.erase(it);
+        in_use -= cls;
+        cached += cls;
+        free_lists[cls].push_back(p);
+    }
+};
+
+// ------------------------------------------------------------ objects
+
+struct PendingGate {
+    int target;
+    std::vector<int> controls;
+    Mat2 m;
+    bool diag;
+};
+
+struct States {
+    int prec;
+    int n_lanes = -1;
+    void *d = nullptr;
+    std::vector<PendingGate> pending;
+};
+
+struct Processor {
+    int prec;
+};
+struct Getter {
+    int prec;
+};
+struct Pool {
+    double *cdf = nullptr;
+    idx_t n = 0;
+    std::vector<int> empty_pos;  // ascending
+};
+
+struct Device {
+    bool initialized = false;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    Arena arena;
+    double *d_partials = nullptr;  // reduce_partials() + 8
+    double *h_result = nullptr;    // pinned, 16 doubles
+    static constexpr size_t kStageBytes = 64ull << 20;
+    void *h_stage[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int tile_lanes[3] = {0, 13, 12};  // indexed by prec: [1] fp64, [2] fp32
+    long long n_gates = 0, n_passes = 0, n_bytes = 0;
+    // Per-kernel-class launch timing with CUDA events on the engine's stream.
+    bool timing = false;
+    struct TimedClass {
+        long long launches = 0;
+        double ms = 0.;
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    };
+    std::map<std::string, TimedClass> timers;
+    std::vector<cudaEvent_t> event_pool;
+    std::unordered_set<States *> states;
+    std::unordered_set<Processor *> procs;
+    std::unordered_set<Getter *> getters;
+    std::unordered_set<Pool *> pools;
+    std::recursive_mutex mu;
+};
+
+static Device g_dev;
+
+static void device_init(int device_id, long long limit) {
+    Device &d = g_dev;
+    if (d.initialized) return;
+    int count = 0;
+    QG_CUDA(cudaGetDeviceCount(&count));
+    if (count < 1) fail(QG_ERR_CUDA, "no CUDA device");
+    if (device_id < 0) QG_CUDA(cudaGetDevice(&device_id));
+    QG_CUDA(cudaSetDevice(device_id));
+    d.dev = device_id;
+    QG_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
+    QG_CUDA(cudaMalloc(&d.d_partials, sizeof(double) * (reduce_partials() + 8)));
+    QG_CUDA(cudaMallocHost(&d.h_result, sizeof(double) * 16));
+    for (int i = 0; i < 2; ++i) {
+        QG_CUDA(cudaMallocHost(&d.h_stage[i], Device::kStageBytes));
+        QG_CUDA(cudaEventCreateWithFlags(&d.ev[i], cudaEventDisableTiming));
+    }
+    d.arena.limit = limit;
+    d.initialized = true;
+}
+
+static Device &dev() {
+    if (!g_dev.initialized) device_init(-1, -1);
+    QG_CUDA(cudaSetDevice(g_dev.dev));
+    return g_dev;
+}
+
+template <class T> static T *lookup(std::unordered_set<T *> &set, qg_handle h, const char *what) {
+    T *p = reinterpret_cast<T *>(h);
+    if (!p || set.find(p) == set.end()) fail(QG_ERR_VALUE, "invalid %s handle.", what);
+    return p;
+}
+static States *get_states(qg_handle h) { return lookup(g_dev.states, h, "qubit states"); }
+static States *get_alloc_states(qg_handle h) {
+    States *s = get_states(h);
+    if (!s->d) fail(QG_ERR_RUNTIME, "qubit states not initialized.");
+    return s;
+}
+
+static void check_lane(const States *s, int lane) {
+    if (lane < 0 || lane >= s->n_lanes)
+        fail(QG_ERR_VALUE, "lane %d out of range [0, %d).", lane, s->n_lanes);
+}
+
+static cudaEvent_t take_event(Device &d) {
+    if (!d.event_pool.empty()) {
+        cudaEvent_t e = d.event_pool.back();
+        d.event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    QG_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+// Runs `launch` (which enqueues kernels on d.stream) and, when timing is on,
+// brackets it with CUDA events attributed to kernel class `cls`.
+template <class F> static void timed(Device &d, const char *cls, F launch) {
+    if (!d.timing) {
+        launch();
+        return;
+    }
+    cudaEvent_t a = take_event(d), b = take_event(d);
+    QG_CUDA(cudaEventRecord(a, d.stream));
+    launch();
+    QG_CUDA(cudaEventRecord(b, d.stream));
+    d.timers[cls].pending.emplace_back(a, b);
+}
+
+static void settle_timers(Device &d) {
+    bool any = false;
+    for (auto &kv : d.timers) any = any || !kv.second.pending.empty();
+    if (!any) return;
+    QG_CUDA(cudaStreamSynchronize(d.stream));
+    for (auto &kv : d.timers) {
+        for (auto &pr : kv.second.pending) {
+            float ms = 0.f;
+            QG_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+            kv.second.ms += ms;
+            kv.second.launches += 1;
+            d.event_pool.push_back(pr.first);
+            d.event_pool.push_back(pr.second);
+        }
+        kv.second.pending.clear();
+    }
+}
+
+// ------------------------------------------------------------ gate queue
+
+static PairIdx pair_pattern(const std::vector<int> &fixed, unsigned long long set_mask,
+                            unsigned long long partner) {
+    PairIdx pi;
+    std::vector<int> pos(fixed);
+    std::sort(pos.begin(), pos.end());
+    pi.npos = (int)pos.size();
+    for (int i = 0; i < pi.npos; ++i) pi.pos[i] = pos[i];
+    pi.set_mask = set_mask;
+    pi.partner = partner;
+    return pi;
+}
+
+static void run_single_gate(Device &d, States *s, const PendingGate &g) {
+    std::vector<int> pos(g.controls);
+    pos.push_back(g.target);
+    unsigned long long cmask = 0;
+    for (int c : g.controls) cmask |= 1ULL << c;
+    PairIdx pi = pair_pattern(pos, cmask, 1ULL << g.target);
+    idx_t n_items = (idx_t)1 << (s->n_lanes - (int)pos.size());
+    timed(d, "gate", [&] { launch_apply_pairs(s->prec, s->d, n_items, pi, g.m, d.stream); });
+    d.n_passes += 1;
+    d.n_bytes += 4 * n_items * (long long)complex_size(s->prec);
+}
+
+static unsigned long long gate_qmask(const PendingGate &g) {
+    unsigned long long q = 1ULL << g.target;
+    for (int c : g.controls) q |= 1ULL << c;
+    return q;
+}
+
+static void run_stage(Device &d, States *s, unsigned long long S,
+                      const std::vector<const PendingGate *> &gates) {
+    StageDesc sd;
+    memset(&sd, 0, sizeof(sd));
+    const int n = s->n_lanes;
+    std::vector<int> lanes;
+    for (int q = 0; q < n; ++q)
+        if (S & (1ULL << q)) lanes.push_back(q);
+    const int m = (int)lanes.size();
+    int local_of[64];
+    for (int i = 0; i < 64; ++i) local_of[i] = -1;
+    for (int i = 0; i < m; ++i) local_of[lanes[i]] = i;
+    sd.n = n;
+    sd.m = m;
+    int lowrun = 0;
+    while (lowrun < m && lanes[lowrun] == lowrun) ++lowrun;
+    sd.lowrun = lowrun;
+    sd.nhi = m - lowrun;
+    for (int j = 0; j < sd.nhi; ++j) sd.hi_pos[j] = lanes[lowrun + j];
+    sd.nins = m < n ? m : 0;
+    for (int j = 0; j < sd.nins; ++j) sd.ins_pos[j] = lanes[j];
+    sd.ngates = (int)gates.size();
+    for (int gi = 0; gi < sd.ngates; ++gi) {
+        const PendingGate &g = *gates[gi];
+        StageGate &G = sd.gates[gi];
+        std::vector<int> pos;
+        unsigned cmask = 0;
+        for (int c : g.controls) {
+            pos.push_back(local_of[c]);
+            cmask |= 1u << local_of[c];
+        }
+        pos.push_back(local_of[g.target]);
+        std::sort(pos.begin(), pos.end());
+        G.npos = (int)pos.size();
+        for (int i = 0; i < G.npos; ++i) G.pos[i] = (signed char)pos[i];
+        G.cmask = cmask;
+        G.tbit = 1u << local_of[g.target];
+        G.diag = g.diag ? 1 : 0;
+        memcpy(G.m, g.m.v, sizeof(G.m));
+    }
+    timed(d, "stage", [&] { launch_stage(s->prec, s->d, sd, d.stream); });
+    d.n_passes += 1;
+    d.n_bytes += 2 * ((long long)1 << n) * (long long)complex_size(s->prec);
+}
+
+// Fusion planner.  Walks the pending gates in order and packs them into
+// stages whose lane set S has at most M lanes; a gate that does not fit, or
+// that touches a lane of an earlier deferred gate, is deferred to the next
+// stage (it then commutes with everything moved ahead of it, because their
+// lane sets are disjoint).  The lowest lanes are always in S so that each
+// tile is made of >= 128-byte contiguous runs.
+static void flush(States *s) {
+    if (s->pending.empty()) return;
+    Device &d = dev();
+    const int n = s->n_lanes;
+    int M = d.tile_lanes[s->prec];
+    std::vector<const PendingGate *> remaining;
+    for (auto &g : s->pending) remaining.push_back(&g);
+    if (M <= 1) {
+        for (auto *g : remaining) run_single_gate(d, s, *g);
+        s->pending.clear();
+        return;
+    }
+    if (M > kMaxTileLanes) M = kMaxTileLanes;
+    const int low = std::min(n, s->prec == kFP32 ? 4 : 3);
+    const unsigned long long all = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+    if (n <= M) M = n;
+    const unsigned long long base = (n <= M) ? all : ((1ULL << low) - 1);
+    while (!remaining.empty()) {
+        unsigned long long S = base, blocked = 0;
+        std::vector<const PendingGate *> chosen, deferred;
+        // A gate wider than a tile runs on its own.
+        if (__builtin_popcountll(gate_qmask(*remaining[0]) | base) > M) {
+            run_single_gate(d, s, *remaining[0]);
+            remaining.erase(remaining.begin());
+            continue;
+        }
+        for (auto *g : remaining) {
+            unsigned long long q = gate_qmask(*g);
+            if ((q & blocked) || (int)chosen.size() >= kMaxStageGates ||
+                __builtin_popcountll(S | q) > M) {
+                deferred.push_back(g);
+                blocked |= q;
+                continue;
+            }
+            S |= q;
+            chosen.push_back(g);
+        }
+        if (chosen.size() == 1) {
+            run_single_gate(d, s, *chosen[0]);
+        } else {
+            for (int q = 0; q < n && __builtin_popcountll(S) < M; ++q) S |= 1ULL << q;
+            run_stage(d, s, S, chosen);
+        }
+        remaining.swap(deferred);
+    }
+    s->pending.clear();
+}
+
+static void flush_all() {
+    for (States *s : g_dev.states) flush(s);
+}
+
+static double read_result(Device &d, double *d_val) {
+    QG_CUDA(cudaMemcpyAsync(d.h_result, d_val, sizeof(double), cudaMemcpyDeviceToHost, d.stream));
+    QG_CUDA(cudaStreamSynchronize(d.stream));
+    return d.h_result[0];
+}
+
+static bool is_diag(const Mat2 &m) {
+    return m.v[2] == 0. && m.v[3] == 0. && m.v[4] == 0. && m.v[5] == 0.;
+}
+
+// ------------------------------------------------------------ transfers
+
+// Device buffer -> host, through two pinned staging buffers so that the
+// host-side copy of one chunk overlaps the transfer of the next.
+// `produce(chunk_begin, chunk_count, dbuf)` fills dbuf on the stream.
+template <class F>
+static void staged_d2h(Device &d, void *host, idx_t count, size_t item, F produce) {
+    if (count <= 0) return;
+    idx_t chunk = (idx_t)(Device::kStageBytes / item);
+    void *dbuf[2] = {d.arena.alloc(chunk * item), nullptr};
+    idx_t nchunks = (count + chunk - 1) / chunk;
+    if (nchunks > 1) dbuf[1] = d.arena.alloc(chunk * item);
+    idx_t pend_begin[2] = {0, 0}, pend_cnt[2] = {0, 0};
+    try {
+        for (idx_t c = 0; c < nchunks + 2; ++c) {
+            int b = (int)(c & 1);
+            if (c >= 2 && pend_cnt[b] > 0) {
+                QG_CUDA(cudaEventSynchronize(d.ev[b]));
+                memcpy((char *)host + pend_begin[b] * item, d.h_stage[b], pend_cnt[b] * item);
+                pend_cnt[b] = 0;
+            }
+            if (c < nchunks) {
+                idx_t begin = c * chunk, cnt = std::min(chunk, count - begin);
+                produce(begin, cnt, dbuf[b]);
+                QG_CUDA(cudaMemcpyAsync(d.h_stage[b], dbuf[b], cnt * item, cudaMemcpyDeviceToHost,
+                                        d.stream));
+                QG_CUDA(cudaEventRecord(d.ev[b], d.stream));
+                pend_begin[b] = begin;
+                pend_cnt[b] = cnt;
+            }
+        }
+    } catch (...) {
+        cudaStreamSynchronize(d.stream);
+        d.arena.release(dbuf[0]);
+        d.arena.release(dbuf[1]);
+        throw;
+    }
+    d.arena.release(dbuf[0]);
+    d.arena.release(dbuf[1]);
+}
+
+// ------------------------------------------------------------ gather descriptors
+
+static GatherDesc make_gather(const int *lane_tables, const int *lane_counts,
+                              const qg_handle *qstates_list, int n_qstates, int prec) {
+    if (n_qstates > kMaxGetterStates) fail(QG_ERR_VALUE, "too many qubit states (%d).", n_qstates);
+    GatherDesc g;
+    memset(&g, 0, sizeof(g));
+    g.nqs = n_qstates;
+    int off = 0;
+    for (int q = 0; q < n_qstates; ++q) {
+        States *s = get_alloc_states(qstates_list[q]);
+        if (s->prec != prec) fail(QG_ERR_VALUE, "precision mismatch between getter and states.");
+        flush(s);
+        if (lane_counts[q] != s->n_lanes)
+            fail(QG_ERR_VALUE, "lane table size %d != n_lanes %d.", lane_counts[q], s->n_lanes);
+        g.ptr[q] = s->d;
+        g.lane_begin[q] = off;
+        for (int l = 0; l < lane_counts[q]; ++l) {
+            if (off >= kMaxLanes) fail(QG_ERR_VALUE, "too many lanes.");
+            int e = lane_tables[off];
+            if (e < 0 || e >= kMaxLanes) fail(QG_ERR_VALUE, "external lane %d out of range.", e);
+            g.ext[off] = (signed char)e;
+            ++off;
+        }
+    }
+    g.lane_begin[n_qstates] = off;
+    return g;
+}
+
+// ------------------------------------------------------------ gate matrices
+
+typedef std::complex<double> cd;
+
+static void put(double *mat, cd a00, cd a01, cd a10, cd a11) {
+    cd v[4] = {a00, a01, a10, a11};
+    for (int i = 0; i < 4; ++i) {
+        mat[2 * i] = v[i].real();
+        mat[2 * i + 1] = v[i].imag();
+    }
+}
+
+// The gate set and conventions of qgate/simulator/src/GateMatrix.cpp:13-158
+// (U = Rz(phi) Ry(theta) Rz(lambda) exactly, i.e. OpenQASM's U up to the
+// global phase exp(i(lambda+phi)/2)).
+static void gate_matrix(const char *name, const double *a, int na, double *mat) {
+    const cd j(0., 1.);
+    const double r = std::sqrt(0.5);
+    auto need = [&](int k) {
+        if (na < k) fail(QG_ERR_VALUE, "gate %s needs %d argument(s).", name, k);
+    };
+    std::string nm(name);
+    if (nm == "U") {
+        need(3);
+        double t2 = a[0] * 0.5, p2 = a[1] * 0.5, l2 = a[2] * 0.5;
+        put(mat, std::exp(j * (-l2 - p2)) * std::cos(t2), -std::exp(j * (l2 - p2)) * std::sin(t2),
+            std::exp(j * (-l2 + p2)) * std::sin(t2), std::exp(j * (l2 + p2)) * std::cos(t2));
+    } else if (nm == "U2") {
+        need(2);
+        double p2 = a[0] * 0.5, l2 = a[1] * 0.5;
+        put(mat, std::exp(j * (-l2 - p2)) * r, -std::exp(j * (l2 - p2)) * r,
+            std::exp(j * (-l2 + p2)) * r, std::exp(j * (l2 + p2)) * r);
+    } else if (nm == "U1") {
+        need(1);
+        put(mat, 1., 0., 0., std::exp(j * a[0]));
+    } else if (nm == "ID") {
+        put(mat, 1., 0., 0., 1.);
+    } else if (nm == "X") {
+        put(mat, 0., 1., 1., 0.);
+    } else if (nm == "Y") {
+        put(mat, 0., -j, j, 0.);
+    } else if (nm == "Z") {
+        put(mat, 1., 0., 0., -1.);
+    } else if (nm == "H") {
+        put(mat, r, r, r, -r);
+    } else if (nm == "S") {
+        put(mat, 1., 0., 0., j);
+    } else if (nm == "T") {
+        put(mat, 1., 0., 0., std::exp(j * (M_PI * 0.25)));
+    } else if (nm == "RX") {
+        need(1);
+        double c = std::cos(a[0] / 2.), s = std::sin(a[0] / 2.);
+        put(mat, c, -j * s, -j * s, c);
+    } else if (nm == "RY") {
+        need(1);
+        double c = std::cos(a[0] / 2.), s = std::sin(a[0] / 2.);
+        put(mat, c, -s, s, c);
+    } else if (nm == "RZ") {
+        need(1);
+        double t2 = a[0] / 2.;
+        put(mat, std::exp(-j * t2), 0., 0., std::exp(j * t2));
+    } else if (nm == "ExpiI") {
+        need(1);
+        cd e = std::exp(j * a[0]);
+        put(mat, e, 0., 0., e);
+    } else if (nm == "ExpiZ") {
+        need(1);
+        put(mat, std::exp(j * a[0]), 0., 0., std::exp(-j * a[0]));
+    } else if (nm == "SH") {
+        put(mat, r, r, j * r, -j * r);
+    } else {
+        fail(QG_ERR_RUNTIME, "Unknown gate type.");
+    }
+}
+
+static void adjoint2(double *m) {
+    // conj(transpose)
+    double t[8];
+    memcpy(t, m, sizeof(t));
+    m[0] = t[0];
+    m[1] = -t[1];
+    m[2] = t[4];
+    m[3] = -t[5];
+    m[4] = t[2];
+    m[5] = -t[3];
+    m[6] = t[6];
+    m[7] = -t[7];
+}
+
+}  // namespace qg
+
+using namespace qg;
+
+#define QG_BEGIN                                      \
+    try {                                             \
+        std::lock_guard<std::recursive_mutex> _lk(g_dev.mu);
+#define QG_END                                                 \
+    }                                                          \
+    catch (const qg::Error &e) {                               \
+        t_last_error = e.msg;                                  \
+        return e.code;                                         \
+    }                                                          \
+    catch (const std::bad_alloc &) {                           \
+        t_last_error = "host allocation failed";               \
+        return QG_ERR_NOMEM;                                   \
+    }                                                          \
+    catch (...) {                                              \
+        t_last_error = "unknown error";                        \
+        return QG_ERR_RUNTIME;                                 \
+    }                                                          \
+    t_last_error.clear();                                      \
+    return QG_OK;
+
+static void check_prec(int prec) {
+    if (prec != kFP64 && prec != kFP32) fail(QG_ERR_VALUE, "unexpected dtype.");
+}
+
+extern "C" {
+
+const char *qg_last_error(void) { return t_last_error.c_str(); }
+
+int qg_devices_initialize(int device_id, int64_t memory_limit) {
+    QG_BEGIN
+    if (g_dev.initialized) {
+        if (device_id >= 0 && device_id != g_dev.dev)
+            fail(QG_ERR_RUNTIME, "already initialized on device %d.", g_dev.dev);
+        g_dev.arena.limit = memory_limit;
+    } else {
+        device_init(device_id, memory_limit);
+    }
+    QG_END
+}
+
+int qg_devices_clear(void) {
+    QG_BEGIN
+    if (g_dev.initialized) {
+        QG_CUDA(cudaSetDevice(g_dev.dev));
+        cudaStreamSynchronize(g_dev.stream);
+        g_dev.arena.trim();
+    }
+    QG_END
+}
+
+int qg_arena_stats(int64_t *in_use, int64_t *cached) {
+    QG_BEGIN
+    *in_use = (int64_t)g_dev.arena.in_use;
+    *cached = (int64_t)g_dev.arena.cached;
+    QG_END
+}
+
+int qg_qubit_states_new(int prec, qg_handle *out) {
+    QG_BEGIN
+    check_prec(prec);
+    States *s = new States();
+    s->prec = prec;
+    g_dev.states.insert(s);
+    *out = (qg_handle)s;
+    QG_END
+}
+
+int qg_qubit_states_delete(qg_handle h) {
+    QG_BEGIN
+    States *s = get_states(h);
+    s->pending.clear();
+    if (s->d) g_dev.arena.release(s->d);
+    g_dev.states.erase(s);
+    delete s;
+    QG_END
+}
+
+int qg_qubit_states_deallocate(qg_handle h) {
+    QG_BEGIN
+    States *s = get_states(h);
+    s->pending.clear();
+    if (s->d) g_dev.arena.release(s->d);
+    s->d = nullptr;
+    s->n_lanes = -1;
+    QG_END
+}
+
+int qg_qubit_states_get_n_lanes(qg_handle h, int *n) {
+    QG_BEGIN
+    *n = get_states(h)->n_lanes;
+    QG_END
+}
+
+int qg_qubit_processor_new(int prec, qg_handle *out) {
+    QG_BEGIN
+    check_prec(prec);
+    Processor *p = new Processor{prec};
+    g_dev.procs.insert(p);
+    *out = (qg_handle)p;
+    QG_END
+}
+
+int qg_qubit_processor_delete(qg_handle h) {
+    QG_BEGIN
+    Processor *p = lookup(g_dev.procs, h, "processor");
+    g_dev.procs.erase(p);
+    delete p;
+    QG_END
+}
+
+int qg_qubit_processor_synchronize(qg_handle h) {
+    QG_BEGIN
+    lookup(g_dev.procs, h, "processor");
+    Device &d = dev();
+    flush_all();
+    QG_CUDA(cudaStreamSynchronize(d.stream));
+    QG_END
+}
+
+int qg_qubit_processor_reset(qg_handle h) {
+    QG_BEGIN
+    lookup(g_dev.procs, h, "processor");
+    QG_END
+}
+
+int qg_qubit_processor_initialize_qubit_states(qg_handle hp, qg_handle hs, int n_lanes) {
+    QG_BEGIN
+    Processor *p = lookup(g_dev.procs, hp, "processor");
+    States *s = get_states(hs);
+    if (p->prec != s->prec) fail(QG_ERR_VALUE, "precision mismatch.");
+    if (n_lanes < 0 || n_lanes > 40) fail(QG_ERR_VALUE, "n_lanes %d out of range.", n_lanes);
+    Device &d = dev();
+    s->pending.clear();
+    if (s->d) d.arena.release(s->d);
+    s->d = nullptr;
+    s->d = d.arena.alloc(((size_t)1 << n_lanes) * complex_size(s->prec));
+    s->n_lanes = n_lanes;
+    QG_END
+}
+
+int qg_qubit_processor_reset_qubit_states(qg_handle hp, qg_handle hs) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    Device &d = dev();
+    s->pending.clear();
+    timed(d, "init", [&] { launch_init_basis(s->prec, s->d, (idx_t)1 << s->n_lanes, d.stream); });
+    QG_END
+}
+
+int qg_qubit_processor_calc_probability(qg_handle hp, qg_handle hs, int lane, double *prob) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    check_lane(s, lane);
+    Device &d = dev();
+    flush(s);
+    PairIdx pi = pair_pattern({lane}, 0, 0);
+    double *d_out = d.d_partials + reduce_partials();
+    timed(d, "prob", [&] {
+        launch_prob(s->prec, s->d, (idx_t)1 << (s->n_lanes - 1), pi, d.d_partials, d_out, d.stream);
+    });
+    *prob = read_result(d, d_out);
+    QG_END
+}
+
+int qg_qubit_processor_join(qg_handle hp, qg_handle hs, const qg_handle *list, int n_list,
+                            int n_new_lanes) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *dst = get_alloc_states(hs);
+    Device &d = dev();
+    if (n_list < 1) fail(QG_ERR_VALUE, "join needs at least one source.");
+    std::vector<const void *> srcs(n_list);
+    std::vector<int> lanes(n_list);
+    int total = 0;
+    for (int i = 0; i < n_list; ++i) {
+        States *s = get_alloc_states(list[i]);
+        if (s == dst) fail(QG_ERR_VALUE, "join destination is also a source.");
+        if (s->prec != dst->prec) fail(QG_ERR_VALUE, "precision mismatch.");
+        flush(s);
+        srcs[i] = s->d;
+        lanes[i] = s->n_lanes;
+        total += s->n_lanes;
+    }
+    if (total + n_new_lanes != dst->n_lanes)
+        fail(QG_ERR_VALUE, "join: %d + %d lanes != %d.", total, n_new_lanes, dst->n_lanes);
+    dst->pending.clear();
+    idx_t prod = (idx_t)1 << total;
+    timed(d, "join", [&] {
+        launch_kron(dst->prec, dst->d, prod, srcs.data(), lanes.data(), n_list, d.stream);
+        launch_fill_zero(dst->prec, dst->d, prod, (idx_t)1 << dst->n_lanes, d.stream);
+    });
+    QG_END
+}
+
+int qg_qubit_processor_decohere(qg_handle hp, int value, double prob, qg_handle hs, int lane) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    check_lane(s, lane);
+    if (value != 0 && value != 1) fail(QG_ERR_VALUE, "value must be 0 or 1.");
+    Device &d = dev();
+    flush(s);
+    double norm = value == 0 ? 1. / std::sqrt(prob) : 1. / std::sqrt(1. - prob);
+    PairIdx pi = pair_pattern({lane}, 0, 1ULL << lane);
+    timed(d, "measure", [&] {
+        launch_decohere(s->prec, s->d, (idx_t)1 << (s->n_lanes - 1), pi, value, norm, d.stream);
+    });
+    QG_END
+}
+
+int qg_qubit_processor_decohere_and_separate(qg_handle hp, int value, double prob,
+                                             qg_handle h0, qg_handle h1, qg_handle hs,
+                                             int lane) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    States *s0 = get_alloc_states(h0);
+    States *s1 = get_alloc_states(h1);
+    check_lane(s, lane);
+    if (value != 0 && value != 1) fail(QG_ERR_VALUE, "value must be 0 or 1.");
+    if (s0->n_lanes != s->n_lanes - 1 || s1->n_lanes != 1)
+        fail(QG_ERR_VALUE, "decohere_and_separate: wrong destination sizes.");
+    if (s0->prec != s->prec || s1->prec != s->prec) fail(QG_ERR_VALUE, "precision mismatch.");
+    Device &d = dev();
+    flush(s);
+    s0->pending.clear();
+    s1->pending.clear();
+    double norm = value == 0 ? 1. / std::sqrt(prob) : 1. / std::sqrt(1. - prob);
+    PairIdx pi = pair_pattern({lane}, (unsigned long long)value << lane, 0);
+    timed(d, "measure", [&] {
+        launch_shrink(s->prec, s0->d, s->d, (idx_t)1 << (s->n_lanes - 1), pi, norm, d.stream);
+    });
+    // qstates1 = |value>
+    launch_init_basis(s1->prec, s1->d, 2, d.stream);
+    if (value == 1) {
+        PairIdx p1 = pair_pattern({0}, 0, 1);
+        Mat2 x = {{0., 0., 1., 0., 1., 0., 0., 0.}};
+        launch_apply_pairs(s1->prec, s1->d, 1, p1, x, d.stream);
+    }
+    QG_END
+}
+
+int qg_qubit_processor_apply_reset(qg_handle hp, qg_handle hs, int lane) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    check_lane(s, lane);
+    Device &d = dev();
+    flush(s);
+    PairIdx pi = pair_pattern({lane}, 0, 1ULL << lane);
+    timed(d, "measure", [&] { launch_reset(s->prec, s->d, (idx_t)1 << (s->n_lanes - 1), pi, d.stream); });
+    QG_END
+}
+
+static void enqueue_gate(qg_handle hp, const double *mat, qg_handle hs, const int *ctrl,
+                         int n_ctrl, int target) {
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    check_lane(s, target);
+    PendingGate g;
+    g.target = target;
+    unsigned long long seen = 1ULL << target;
+    for (int i = 0; i < n_ctrl; ++i) {
+        check_lane(s, ctrl[i]);
+        if (seen & (1ULL << ctrl[i])) fail(QG_ERR_RUNTIME, "control and operand overlapped.");
+        seen |= 1ULL << ctrl[i];
+        g.controls.push_back(ctrl[i]);
+    }
+    memcpy(g.m.v, mat, sizeof(g.m.v));
+    g.diag = is_diag(g.m);
+    s->pending.push_back(g);
+    g_dev.n_gates += 1;
+}
+
+int qg_qubit_processor_apply_gate(qg_handle hp, const double *mat, qg_handle hs, int lane) {
+    QG_BEGIN
+    enqueue_gate(hp, mat, hs, nullptr, 0, lane);
+    QG_END
+}
+
+int qg_qubit_processor_apply_controlled_gate(qg_handle hp, const double *mat, qg_handle hs,
+                                             const int *ctrl, int n_ctrl, int target) {
+    QG_BEGIN
+    enqueue_gate(hp, mat, hs, ctrl, n_ctrl, target);
+    QG_END
+}
+
+int qg_qubit_processor_apply_multi(qg_handle hp, const double *mat, qg_handle hs,
+                                   const int *targets, int n_targets, const int *ctrl,
+                                   int n_ctrl) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    if (n_targets < 1 || n_targets > 5) fail(QG_ERR_VALUE, "1..5 targets supported.");
+    MultiDesc md;
+    memset(&md, 0, sizeof(md));
+    md.k = n_targets;
+    unsigned long long seen = 0;
+    std::vector<int> pos;
+    for (int i = 0; i < n_targets; ++i) {
+        check_lane(s, targets[i]);
+        if (seen & (1ULL << targets[i])) fail(QG_ERR_VALUE, "duplicate target lane.");
+        seen |= 1ULL << targets[i];
+        md.tpos[i] = targets[i];
+        pos.push_back(targets[i]);
+    }
+    for (int i = 0; i < n_ctrl; ++i) {
+        check_lane(s, ctrl[i]);
+        if (seen & (1ULL << ctrl[i])) fail(QG_ERR_RUNTIME, "control and operand overlapped.");
+        seen |= 1ULL << ctrl[i];
+        md.cmask |= 1ULL << ctrl[i];
+        pos.push_back(ctrl[i]);
+    }
+    std::sort(pos.begin(), pos.end());
+    md.npos = (int)pos.size();
+    for (int i = 0; i < md.npos; ++i) md.pos[i] = pos[i];
+    Device &d = dev();
+    flush(s);
+    size_t dim = (size_t)1 << n_targets;
+    size_t bytes = dim * dim * 2 * sizeof(double);
+    void *dmat = d.arena.alloc(bytes);
+    QG_CUDA(cudaMemcpyAsync(dmat, mat, bytes, cudaMemcpyHostToDevice, d.stream));
+    idx_t n_items = (idx_t)1 << (s->n_lanes - md.npos);
+    timed(d, "multi", [&] { launch_apply_multi(s->prec, s->d, n_items, md, dmat, d.stream); });
+    // The host matrix may be reused by the caller as soon as we return.
+    QG_CUDA(cudaStreamSynchronize(d.stream));
+    d.arena.release(dmat);
+    d.n_gates += 1;
+    d.n_passes += 1;
+    d.n_bytes += 2 * ((long long)n_items << n_targets) * (long long)complex_size(s->prec);
+    QG_END
+}
+
+int qg_qubit_processor_calc_pauli_expectation(qg_handle hp, qg_handle hs, uint64_t x_mask,
+                                              uint64_t z_mask, double *out) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    unsigned long long all = s->n_lanes >= 64 ? ~0ULL : ((1ULL << s->n_lanes) - 1);
+    if ((x_mask | z_mask) & ~all) fail(QG_ERR_VALUE, "Pauli mask outside the state's lanes.");
+    Device &d = dev();
+    flush(s);
+    double *d_out = d.d_partials + reduce_partials();
+    timed(d, "pauli", [&] {
+        launch_pauli(s->prec, s->d, s->n_lanes, x_mask, z_mask, d.d_partials, d_out, d.stream);
+    });
+    *out = read_result(d, d_out);
+    QG_END
+}
+
+int qg_qubit_processor_calc_norm(qg_handle hp, qg_handle hs, double *out) {
+    QG_BEGIN
+    lookup(g_dev.procs, hp, "processor");
+    States *s = get_alloc_states(hs);
+    Device &d = dev();
+    flush(s);
+    double *d_out = d.d_partials + reduce_partials();
+    launch_pauli(s->prec, s->d, s->n_lanes, 0, 0, d.d_partials, d_out, d.stream);
+    *out = read_result(d, d_out);
+    QG_END
+}
+
+int qg_set_fusion(int max_tile_lanes) {
+    QG_BEGIN
+    if (max_tile_lanes < 0 || max_tile_lanes > kMaxTileLanes)
+        fail(QG_ERR_VALUE, "max_tile_lanes must be in [0, %d].", kMaxTileLanes);
+    flush_all();
+    if (max_tile_lanes == 0) {
+        g_dev.tile_lanes[kFP32] = 13;
+        g_dev.tile_lanes[kFP64] = 12;
+    } else {
+        g_dev.tile_lanes[kFP32] = max_tile_lanes;
+        g_dev.tile_lanes[kFP64] = std::min(max_tile_lanes, 13);
+    }
+    QG_END
+}
+
+int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset) {
+    QG_BEGIN
+    *gates = g_dev.n_gates;
+    *passes = g_dev.n_passes;
+    *bytes = g_dev.n_bytes;
+    if (reset) g_dev.n_gates = g_dev.n_passes = g_dev.n_bytes = 0;
+    QG_END
+}
+
+int qg_qubit_states_get_raw(qg_handle hs, void *host, int64_t n) {
+    QG_BEGIN
+    States *s = get_alloc_states(hs);
+    if (n != ((int64_t)1 << s->n_lanes)) fail(QG_ERR_VALUE, "size mismatch.");
+    Device &d = dev();
+    flush(s);
+    size_t cs = complex_size(s->prec);
+    staged_d2h(d, host, n, cs, [&](idx_t begin, idx_t cnt, void *dbuf) {
+        QG_CUDA(cudaMemcpyAsync(dbuf, (char *)s->d + begin * cs, cnt * cs,
+                                cudaMemcpyDeviceToDevice, d.stream));
+    });
+    QG_END
+}
+
+int qg_qubit_states_set_raw(qg_handle hs, const void *host, int64_t n) {
+    QG_BEGIN
+    States *s = get_alloc_states(hs);
+    if (n != ((int64_t)1 << s->n_lanes)) fail(QG_ERR_VALUE, "size mismatch.");
+    Device &d = dev();
+    s->pending.clear();
+    QG_CUDA(cudaMemcpyAsync(s->d, host, n * complex_size(s->prec), cudaMemcpyHostToDevice,
+                            d.stream));
+    QG_CUDA(cudaStreamSynchronize(d.stream));
+    QG_END
+}
+
+int qg_timing_enable(int on) {
+    QG_BEGIN
+    Device &d = dev();
+    if (!on) settle_timers(d);
+    d.timing = on != 0;
+    QG_END
+}
+
+int qg_timing_read(const char *kernel_class, int64_t *launches, double *total_ms, int reset) {
+    QG_BEGIN
+    Device &d = dev();
+    settle_timers(d);
+    auto it = d.timers.find(kernel_class ? kernel_class : "");
+    *launches = it == d.timers.end() ? 0 : it->second.launches;
+    *total_ms = it == d.timers.end() ? 0. : it->second.ms;
+    if (reset) d.timers.clear();
+    QG_END
+}
+
+int qg_device_info(int64_t *info, int n) {
+    QG_BEGIN
+    Device &d = dev();
+    const cudaDeviceAttr attrs[] = {cudaDevAttrMultiProcessorCount,
+                                    cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                    cudaDevAttrL2CacheSize,
+                                    cudaDevAttrPageableMemoryAccess,
+                                    cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                    cudaDevAttrConcurrentManagedAccess,
+                                    cudaDevAttrComputeCapabilityMajor,
+                                    cudaDevAttrComputeCapabilityMinor,
+                                    cudaDevAttrClockRate,
+                                    cudaDevAttrMemoryClockRate};
+    const int na = (int)(sizeof(attrs) / sizeof(attrs[0]));
+    for (int i = 0; i < n && i < na; ++i) {
+        int v = 0;
+        QG_CUDA(cudaDeviceGetAttribute(&v, attrs[i], d.dev));
+        info[i] = v;
+    }
+    size_t fr = 0, tot = 0;
+    QG_CUDA(cudaMemGetInfo(&fr, &tot));
+    if (n > na) info[na] = (int64_t)fr;
+    if (n > na + 1) info[na + 1] = (int64_t)tot;
+    QG_END
+}
+
+int qg_get_stream(uint64_t *stream) {
+    QG_BEGIN
+    *stream = (uint64_t)(uintptr_t)dev().stream;
+    QG_END
+}
+
+int qg_gate_matrix(const char *name, const double *args, int n_args, int adjoint, double *mat) {
+    QG_BEGIN
+    if (!name) fail(QG_ERR_VALUE, "null gate name.");
+    gate_matrix(name, args, n_args, mat);
+    if (adjoint) adjoint2(mat);
+    QG_END
+}
+
+int qg_qubits_states_getter_new(int prec, qg_handle *out) {
+    QG_BEGIN
+    check_prec(prec);
+    Getter *g = new Getter{prec};
+    g_dev.getters.insert(g);
+    *out = (qg_handle)g;
+    QG_END
+}
+
+int qg_qubits_states_getter_delete(qg_handle h) {
+    QG_BEGIN
+    Getter *g = lookup(g_dev.getters, h, "getter");
+    g_dev.getters.erase(g);
+    delete g;
+    QG_END
+}
+
+int qg_qubits_states_getter_get_states(qg_handle hg, void *values, int64_t array_offset,
+                                       int mathop, const int *lane_tables,
+                                       const int *lane_counts, const qg_handle *qstates_list,
+                                       int n_qstates, uint64_t empty_lane_mask, int n_qregs,
+                                       int64_t n_states, int64_t start, int64_t step) {
+    QG_BEGIN
+    Getter *g = lookup(g_dev.getters, hg, "getter");
+    if (mathop != QG_MATHOP_NULL && mathop != QG_MATHOP_PROB) fail(QG_ERR_RUNTIME, "Unknown math op.");
+    if (n_qregs < 0 || n_qregs > kMaxLanes) fail(QG_ERR_VALUE, "value out of range");
+    long long size = 1LL << n_qregs;
+    if (n_states <= 0) {
+        t_last_error.clear();
+        return QG_OK;
+    }
+    if (start < 0 || size <= start) fail(QG_ERR_VALUE, "value out of range");
+    long long end = start + step * (n_states - 1);
+    if (end < 0 || size <= end) fail(QG_ERR_VALUE, "value out of range");
+    size_t rs = g->prec == kFP64 ? 8 : 4;
+    size_t item = mathop == QG_MATHOP_NULL ? 2 * rs : rs;
+    char *dst = (char *)values + array_offset * item;
+    if (n_qstates == 0) {
+        // no states: |0...0> of the empty lanes (qgate/simulator/src/glue.cpp:480-495)
+        memset(dst, 0, n_states * item);
+        if (start == 0) {
+            if (rs == 4)
+                *(float *)dst = 1.f;
+            else
+                *(double *)dst = 1.;
+        }
+        t_last_error.clear();
+        return QG_OK;
+    }
+    GatherDesc gd = make_gather(lane_tables, lane_counts, qstates_list, n_qstates, g->prec);
+    Device &d = dev();
+    staged_d2h(d, dst, n_states, item, [&](idx_t begin, idx_t cnt, void *dbuf) {
+        timed(d, "gather", [&] {
+            launch_gather(g->prec, mathop, dbuf, cnt, start + step * begin, step, empty_lane_mask,
+                          gd, d.stream);
+        });
+    });
+    QG_END
+}
+
+static double *marginal_to_device(Device &d, Getter *g, const int *lane_tables,
+                                  const int *lane_counts, const qg_handle *qstates_list,
+                                  int n_qstates, int n_lanes, int n_hidden) {
+    if (n_lanes < 0 || n_hidden < 0 || n_lanes + n_hidden > kMaxLanes)
+        fail(QG_ERR_VALUE, "lane counts out of range.");
+    GatherDesc gd = make_gather(lane_tables, lane_counts, qstates_list, n_qstates, g->prec);
+    int total = gd.lane_begin[n_qstates];
+    if (total != n_lanes + n_hidden) fail(QG_ERR_VALUE, "lane tables do not cover all lanes.");
+    idx_t n_out = (idx_t)1 << n_lanes;
+    double *prob = (double *)d.arena.alloc(n_out * sizeof(double));
+    size_t sc = marginal_scratch_doubles(n_lanes, n_hidden);
+    double *scratch = sc ? (double *)d.arena.alloc(sc * sizeof(double)) : nullptr;
+    timed(d, "marginal",
+          [&] { launch_marginal(g->prec, prob, n_lanes, n_hidden, gd, scratch, sc, d.stream); });
+    if (scratch) d.arena.release(scratch);  // stream-ordered reuse is safe
+    return prob;
+}
+
+int qg_qubits_states_getter_prepare_prob_array(qg_handle hg, void *prob, const int *lane_tables,
+                                               const int *lane_counts,
+                                               const qg_handle *qstates_list, int n_qstates,
+                                               int n_lanes, int n_hidden_lanes) {
+    QG_BEGIN
+    Getter *g = lookup(g_dev.getters, hg, "getter");
+    Device &d = dev();
+    double *dprob = marginal_to_device(d, g, lane_tables, lane_counts, qstates_list, n_qstates,
+                                       n_lanes, n_hidden_lanes);
+    idx_t n_out = (idx_t)1 << n_lanes;
+    size_t rs = g->prec == kFP64 ? 8 : 4;
+    try {
+        staged_d2h(d, prob, n_out, rs, [&](idx_t begin, idx_t cnt, void *dbuf) {
+            launch_convert_f64(g->prec, dbuf, dprob + begin, cnt, d.stream);
+        });
+    } catch (...) {
+        d.arena.release(dprob);
+        throw;
+    }
+    d.arena.release(dprob);
+    QG_END
+}
+
+int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_tables,
+                                                 const int *lane_counts,
+                                                 const qg_handle *qstates_list, int n_qstates,
+                                                 int n_lanes, int n_hidden_lanes,
+                                                 const int *empty_lanes, int n_empty,
+                                                 qg_handle *out) {
+    QG_BEGIN
+    Getter *g = lookup(g_dev.getters, hg, "getter");
+    Device &d = dev();
+    if (n_empty < 0 || n_lanes + n_empty > kMaxLanes) fail(QG_ERR_VALUE, "too many empty lanes.");
+    double *cdf = marginal_to_device(d, g, lane_tables, lane_counts, qstates_list, n_qstates,
+                                     n_lanes, n_hidden_lanes);
+    idx_t n = (idx_t)1 << n_lanes;
+    size_t sc = scan_scratch_doubles(n);
+    double *scratch = nullptr;
+    try {
+        scratch = (double *)d.arena.alloc(sc * sizeof(double));
+        double *d_total = d.d_partials + reduce_partials();
+        timed(d, "scan", [&] { launch_scan_sums(cdf, n, scratch, d_total, d.stream); });
+        double total = read_result(d, d_total);
+        // qgate/simulator/src/CPUSamplingPool.cpp:31-32
+        if (!(std::fabs(total - 1.) <= 0.05))
+            fail(QG_ERR_RUNTIME, "error in probability sum is beyond 0.05., %g.", total);
+        timed(d, "scan", [&] { launch_scan_apply(cdf, n, scratch, 1. / total, d.stream); });
+    } catch (...) {
+        if (scratch) d.arena.release(scratch);
+        d.arena.release(cdf);
+        throw;
+    }
+    d.arena.release(scratch);
+    Pool *p = new Pool();
+    p->cdf = cdf;
+    p->n = n;
+    for (int i = 0; i < n_empty; ++i) p->empty_pos.push_back(empty_lanes[i]);
+    std::sort(p->empty_pos.begin(), p->empty_pos.end());
+    g_dev.pools.insert(p);
+    *out = (qg_handle)p;
+    QG_END
+}
+
+int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
+                            const double *randnum) {
+    QG_BEGIN
+    Pool *p = lookup(g_dev.pools, hp, "sampling pool");
+    if (n_samples < 0) fail(QG_ERR_VALUE, "negative sample count.");
+    if (n_samples == 0) {
+        t_last_error.clear();
+        return QG_OK;
+    }
+    Device &d = dev();
+    // Uniforms go up through staging buffer 0, indices come back through 1.
+    idx_t chunk = (idx_t)(Device::kStageBytes / 8);
+    double *du = (double *)d.arena.alloc(chunk * 8);
+    long long *dobs = (long long *)d.arena.alloc(chunk * 8);
+    try {
+        for (idx_t b = 0; b < n_samples; b += chunk) {
+            idx_t cnt = std::min(chunk, (idx_t)n_samples - b);
+            memcpy(d.h_stage[0], randnum + b, cnt * 8);
+            QG_CUDA(cudaMemcpyAsync(du, d.h_stage[0], cnt * 8, cudaMemcpyHostToDevice, d.stream));
+            timed(d, "search", [&] {
+                launch_search(p->cdf, p->n, du, dobs, cnt, p->empty_pos.data(),
+                              (int)p->empty_pos.size(), d.stream);
+            });
+            QG_CUDA(cudaMemcpyAsync(d.h_stage[1], dobs, cnt * 8, cudaMemcpyDeviceToHost, d.stream));
+            QG_CUDA(cudaStreamSynchronize(d.stream));
+            memcpy(obs + b, d.h_stage[1], cnt * 8);
+        }
+    } catch (...) {
+        d.arena.release(du);
+        d.arena.release(dobs);
+        throw;
+    }
+    d.arena.release(du);
+    d.arena.release(dobs);
+    QG_END
+}
+
+int qg_sampling_pool_delete(qg_handle hp) {
+    QG_BEGIN
+    Pool *p = lookup(g_dev.pools, hp, "sampling pool");
+    g_dev.arena.release(p->cdf);
+    g_dev.pools.erase(p);
+    delete p;
+    QG_END
+}
+
+}  // extern "C"

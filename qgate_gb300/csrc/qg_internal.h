@@ -1,0 +1,141 @@
+// Internal declarations shared by the engine's translation units.
+//
+// State layout in HBM: one contiguous buffer of 2^n interleaved complex
+// amplitudes (float2 for complex64, double2 for complex128); bit i of an
+// amplitude index is local lane i.  This is the reference's layout
+// (qgate/simulator/src/DeviceTypes.h:18-58), kept so that lane numbering and
+// index conventions are identical; the reference's multi-device chunking
+// (qgate/simulator/src/MultiChunkPtr.h:28-41) is dropped: one GPU holds the
+// whole state in a single allocation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+namespace qg {
+
+typedef long long idx_t;
+
+constexpr int kMaxLanes = 62;        // index bits an amplitude index may carry
+constexpr int kMaxStageGates = 96;   // gates one fused stage may apply
+constexpr int kMaxTileLanes = 14;    // lanes one shared-memory tile may hold
+constexpr int kMaxGetterStates = 63; // states objects one gather may combine
+constexpr int kMaxMultiTargets = 6;  // targets of a dense multi-target gate
+
+enum Prec { kFP64 = 1, kFP32 = 2 };
+
+inline size_t complex_size(int prec) { return prec == kFP64 ? 16 : 8; }
+
+// Thrown inside the engine, caught at the extern "C" boundary.
+struct Error {
+    int code;
+    std::string msg;
+};
+[[noreturn]] void fail(int code, const char *fmt, ...);
+void cuda_check(cudaError_t err, const char *what);
+#define QG_CUDA(call) ::qg::cuda_check((call), #call)
+
+// ---------------------------------------------------------------- kernels
+
+// Pair-sweep index pattern: the k-th work item is the amplitude index made by
+// inserting zero bits at pos[0..npos) (ascending) into k, then OR-ing
+// set_mask; its partner is that index | partner.
+struct PairIdx {
+    int npos;
+    int pos[kMaxLanes];
+    unsigned long long set_mask;
+    unsigned long long partner;
+};
+
+// Row-major 2x2 complex matrix in FP64 (converted to the state's precision
+// inside the kernels, as the reference does:
+// qgate/simulator/src/CPUQubitProcessor.cpp:311).
+struct Mat2 {
+    double v[8];
+};
+
+// One gate of a fused stage, in tile-local lane numbering.
+struct StageGate {
+    int npos;               // inserted zero bits (controls + target)
+    signed char pos[kMaxTileLanes];
+    unsigned cmask;         // tile-local control bits
+    unsigned tbit;          // tile-local target bit
+    int diag;               // matrix is diagonal
+    double m[8];
+};
+
+struct StageDesc {
+    int n;                  // lanes of the state
+    int m;                  // lanes per tile
+    int lowrun;             // tile lanes 0..lowrun-1 are global lanes 0..lowrun-1
+    int nhi;                // tile lanes lowrun..m-1
+    int hi_pos[kMaxTileLanes];       // their global lanes
+    int nins;               // = m when m < n: global lanes of the tile, ascending
+    int ins_pos[kMaxTileLanes];
+    int ngates;
+    StageGate gates[kMaxStageGates];
+};
+
+// Descriptor of a lane-permuted gather over a product of states.
+struct GatherDesc {
+    int nqs;
+    const void *ptr[kMaxGetterStates];
+    int lane_begin[kMaxGetterStates + 1];  // into ext[]
+    signed char ext[kMaxLanes + 2];        // external bit of each local lane
+};
+
+// Dense multi-target gate descriptor.
+struct MultiDesc {
+    int k;                       // targets
+    int tpos[kMaxMultiTargets];  // target lanes (matrix bit order)
+    int npos;                    // sorted insertion positions (targets + controls)
+    int pos[kMaxLanes];
+    unsigned long long cmask;
+};
+
+// All launchers run asynchronously on `stream`.
+void launch_init_basis(int prec, void *state, idx_t n_amps, cudaStream_t stream);
+void launch_fill_zero(int prec, void *state, idx_t begin, idx_t end, cudaStream_t stream);
+void launch_apply_pairs(int prec, void *state, idx_t n_items, const PairIdx &pi, const Mat2 &m,
+                        cudaStream_t stream);
+void launch_decohere(int prec, void *state, idx_t n_items, const PairIdx &pi, int value,
+                     double norm, cudaStream_t stream);
+void launch_reset(int prec, void *state, idx_t n_items, const PairIdx &pi, cudaStream_t stream);
+void launch_shrink(int prec, void *dst, const void *src, idx_t n_items, const PairIdx &pi,
+                   double norm, cudaStream_t stream);
+void launch_kron(int prec, void *dst, idx_t n_dst, const void *const *srcs, const int *src_lanes,
+                 int n_src, cudaStream_t stream);
+void launch_apply_multi(int prec, void *state, idx_t n_items, const MultiDesc &d,
+                        const void *d_mat, cudaStream_t stream);
+void launch_stage(int prec, void *state, const StageDesc &d, cudaStream_t stream);
+
+// Reductions: write one FP64 value to d_out (device), using d_partials as
+// scratch of at least reduce_partials() doubles.
+int reduce_partials();
+void launch_prob(int prec, const void *state, idx_t n_items, const PairIdx &pi,
+                 double *d_partials, double *d_out, cudaStream_t stream);
+void launch_pauli(int prec, const void *state, int n_lanes, unsigned long long x_mask,
+                  unsigned long long z_mask, double *d_partials, double *d_out,
+                  cudaStream_t stream);
+
+// Getter / pool.
+void launch_gather(int prec, int mathop, void *out, idx_t count, idx_t start, idx_t step,
+                   unsigned long long empty_mask, const GatherDesc &g, cudaStream_t stream);
+// Marginal probabilities (FP64) over 2^n_lanes outputs with n_hidden hidden
+// lanes placed above them in the external index.
+void launch_marginal(int prec, double *out, int n_lanes, int n_hidden, const GatherDesc &g,
+                     double *d_scratch, size_t scratch_doubles, cudaStream_t stream);
+size_t marginal_scratch_doubles(int n_lanes, int n_hidden);
+void launch_convert_f64(int prec, void *dst, const double *src, idx_t n, cudaStream_t stream);
+// In-place inclusive FP64 scan; returns the total through d_total.
+size_t scan_scratch_doubles(idx_t n);
+void launch_scan_sums(double *data, idx_t n, double *d_scratch, double *d_total,
+                      cudaStream_t stream);
+void launch_scan_apply(double *data, idx_t n, double *d_scratch, double norm,
+                       cudaStream_t stream);
+void launch_search(const double *cdf, idx_t n, const double *u, long long *obs, idx_t n_samples,
+                   const int *empty_pos, int n_empty, cudaStream_t stream);
+
+}  // namespace qg

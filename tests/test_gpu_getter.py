@@ -1,0 +1,157 @@
+"""GPU parity of the lane-permuted gather, the marginal probability array and
+the FP64 sampling pool against the oracle, plus the reference's own
+known-answer sampling tests (tests/test_sampling_pool.py in the reference:
+midpoint uniforms on the uniform state give the identity indices; empty lanes
+read 0; hidden lanes are summed out)."""
+import numpy as np
+import pytest
+
+from oracle import statevec as sv
+from tests.gpu_helpers import ATOL, Lane, abs2, apply_ops, new_state, null, random_ops
+
+pytestmark = pytest.mark.gpu
+
+DTYPES = [np.float64, np.float32]
+IDS = ['c128', 'c64']
+
+
+def _build(rt, dtype, sizes, seed):
+    rng = np.random.default_rng(seed)
+    states, psis = [], []
+    for k in sizes:
+        ops = random_ops(rng, k, 15)
+        qs = new_state(rt, k, dtype)
+        apply_ops(qs, ops)
+        states.append(qs)
+        psis.append(sv.run_ops(k, ops, np.complex128))
+    return rng, states, psis
+
+
+def _lane_trans(states, tables):
+    return [(qs, [Lane(l, e) for l, e in enumerate(t)]) for qs, t in zip(states, tables)]
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_get_states_permuted_empty_slices(rt, dtype):
+    sizes = [3, 2, 4]
+    rng, states, psis = _build(rt, dtype, sizes, 11)
+    n_lanes = sum(sizes)
+    empty = [1, 7]
+    n_qregs = n_lanes + len(empty)
+    ext = [e for e in rng.permutation(n_qregs) if e not in empty]
+    tables, i = [], 0
+    for k in sizes:
+        tables.append([int(e) for e in ext[i:i + k]])
+        i += k
+    mask = (1 << 1) | (1 << 7)
+    N = 1 << n_qregs
+    getter = rt.create_qubits_states_getter(dtype)
+    for mathop, name in ((null, 'null'), (abs2, 'abs2')):
+        for start, step, count in ((0, 1, N), (5, 3, (N - 5 + 2) // 3), (N - 1, -1, N),
+                                   (N - 2, -7, 100), (17, 1, 1)):
+            vd = (np.complex128 if dtype == np.float64 else np.complex64) if name == 'null' \
+                else dtype
+            values = np.zeros(count + 3, vd)
+            getter.get_states(values, 3, mathop, _lane_trans(states, tables), empty, count, start,
+                              step)
+            want = sv.get_states(list(zip(psis, tables)), name, count, start, step, mask)
+            assert np.allclose(values[3:], want, atol=ATOL[dtype] * 2), (name, start, step)
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_get_states_range_errors(rt, dtype):
+    _, states, _ = _build(rt, dtype, [3], 12)
+    getter = rt.create_qubits_states_getter(dtype)
+    values = np.zeros(16, dtype)
+    lt = _lane_trans(states, [[0, 1, 2]])
+    with pytest.raises(ValueError):
+        getter.get_states(values, 0, abs2, lt, [], 4, 6, 1)   # end beyond 2^3
+    with pytest.raises(ValueError):
+        getter.get_states(values, 0, abs2, _lane_trans(states, [[0, 1, 2]]), [], 2, 8, 1)
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_marginal_probabilities_hidden_lanes(rt, dtype):
+    """Pool over a permuted subset of lanes of two states; the other lanes
+    are hidden and summed out (placed above the pool lanes, in order of
+    appearance, as the runtime does)."""
+    sizes = [5, 4]
+    rng, states, psis = _build(rt, dtype, sizes, 13)
+    n_total = sum(sizes)
+    getter = rt.create_qubits_states_getter(dtype)
+    for n_pool in (1, 3, 6, 9):
+        chosen = rng.permutation(n_total)[:n_pool]   # global lane -> pool position
+        pos = {int(g): j for j, g in enumerate(chosen)}
+        tables, g = [], 0
+        for k in sizes:
+            tables.append([pos.get(g + q, -1) for q in range(k)])
+            g += k
+        captured = {}
+
+        def factory(prob, empty_lanes, ordering):
+            captured['p'] = prob
+        getter.create_sampling_pool(list(range(n_pool)), n_pool, n_total - n_pool,
+                                    _lane_trans(states, tables), [], factory)
+        h, otables = n_pool, []
+        for t in tables:
+            row = []
+            for e in t:
+                if e == -1:
+                    row.append(h)
+                    h += 1
+                else:
+                    row.append(e)
+            otables.append(row)
+        want = sv.marginal_probabilities(list(zip(psis, otables)), n_pool, n_total - n_pool)
+        assert captured['p'].dtype == dtype
+        assert np.allclose(captured['p'], want, atol=ATOL[dtype] * 2), n_pool
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_sampling_pool_midpoints_identity_24q(rt, dtype):
+    """The reference's golden-vector test at its CUDA size (24 qubits):
+    H on every qubit, uniforms at bin midpoints (k + 1/2)/2^n -> index k."""
+    n = 24
+    qs = new_state(rt, n, dtype)
+    apply_ops(qs, [('g', 'H', (), False, q, ()) for q in range(n)])
+    getter = rt.create_qubits_states_getter(dtype)
+    lt = _lane_trans([qs], [list(range(n))])
+    pool = getter.create_sampling_pool(list(range(n)), n, 0, lt, [])
+    N = 1 << n
+    u = (np.arange(N, dtype=np.float64) + 0.5) / N
+    obs = pool.sample(N, u)
+    assert np.array_equal(np.asarray(obs.intarray), np.arange(N))
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_sampling_pool_empty_lanes_and_random(rt, dtype):
+    sizes = [6]
+    rng, states, psis = _build(rt, dtype, sizes, 14)
+    getter = rt.create_qubits_states_getter(dtype)
+    empty = [0, 4, 8]
+    # pool lanes are numbered 0..5; zero bits for the empty lanes are inserted
+    # into each sampled index
+    lt = _lane_trans(states, [list(range(6))])
+    pool = getter.create_sampling_pool(list(range(9)), 6, 0, lt, empty)
+    u = rng.random(20000)
+    got = np.asarray(pool.sample(len(u), u).intarray)
+    prob = sv.marginal_probabilities(list(zip(psis, [list(range(6))])), 6, 0)
+    want = sv.SamplingPool(prob, empty).sample(u)
+    bad = got != want
+    if bad.any():
+        cdf_ref = np.cumsum(prob) / prob.sum()
+        # only uniforms within float rounding of a boundary may differ
+        assert np.all(np.abs(u[bad][:, None] - cdf_ref[None, :]).min(axis=1) < 1e-6)
+    assert np.all((got & ((1 << 0) | (1 << 4) | (1 << 8))) == 0)
+
+
+def test_sampling_pool_rejects_unnormalised_state(rt):
+    """|sum - 1| > 0.05 raises, as CPUSamplingPool does
+    (qgate/simulator/src/CPUSamplingPool.cpp:31-32)."""
+    qs = new_state(rt, 4, np.float64)
+    # decohere with a wrong probability leaves the state unnormalised
+    qs.processor.decohere(0, 0.5, qs, 0)
+    getter = rt.create_qubits_states_getter(np.float64)
+    lt = _lane_trans([qs], [list(range(4))])
+    with pytest.raises(RuntimeError, match='beyond 0.05'):
+        getter.create_sampling_pool(list(range(4)), 4, 0, lt, [])
