@@ -162,6 +162,28 @@ int qg_get_stream(uint64_t *stream);
 int qg_qubit_states_get_raw(qg_handle qstates, void *host, int64_t n);
 int qg_qubit_states_set_raw(qg_handle qstates, const void *host, int64_t n);
 
+/* ---- allocation-free variant ------------------------------------------- */
+
+/* No counterpart in the reference.  Pr(local_lane == 0) of a state held in
+ * caller-owned device memory (2^n_lanes complex64 for QG_PREC_FP32,
+ * complex128 for QG_PREC_FP64), written as one double to caller-owned device
+ * memory d_prob, enqueued on `stream` (a cudaStream_t; 0 = legacy default
+ * stream) and returning before it completes.  For callers that cannot let
+ * the library allocate: code that keeps all device memory in its own
+ * pre-sized pool, or loops that must not take the device-wide
+ * synchronisation a cudaMalloc / cudaFree can imply.  It allocates nothing
+ * and never touches the engine's own context: the reduction's per-block
+ * partials go to a fixed 1024-double (8 KiB) device array that each GPU
+ * holds from library load until process exit.  The reduction uses at most
+ * 608 of those partials for any state size; n_lanes must be in [1, 40] and
+ * anything else is rejected with QG_ERR_VALUE.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current, so make that first call before any stream capture.  All
+ * calls share the one array: calls whose work overlaps on the GPU (different
+ * streams, no ordering between them) race on it and give wrong results. */
+int qg_calc_probability_noalloc(int prec, const void *d_state, int n_lanes, int local_lane,
+                                double *d_prob, uint64_t stream);
+
 /* ---- gate matrices (qgate/simulator/src/GateMatrix.cpp:13-158) --------- */
 
 /* Replaces glue.register_matrix_factory + the MatFactory call in

@@ -61,6 +61,7 @@ SIGNATURES = {
     'qg_qubit_states_get_raw': [_h, _vp, _i64],
     'qg_qubit_states_set_raw': [_h, _vp, _i64],
     'qg_gate_matrix': [ctypes.c_char_p, _dp, _i, _i, _dp],
+    'qg_calc_probability_noalloc': [_i, _vp, _i, _i, _vp, _u64],
     'qg_qubits_states_getter_new': [_i, _hp],
     'qg_qubits_states_getter_delete': [_h],
     'qg_qubits_states_getter_get_states': [_h, _vp, _i64, _i, _ip, _ip, _hp, _i, _u64, _i,

@@ -28,6 +28,8 @@ namespace qg {
 
 static thread_local std::string t_last_error;
 
+void set_last_error(const std::string &msg) { t_last_error = msg; }
+
 void fail(int code, const char *fmt, ...) {
     char buf[512];
     va_list ap;

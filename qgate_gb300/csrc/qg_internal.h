@@ -35,6 +35,8 @@ struct Error {
 };
 [[noreturn]] void fail(int code, const char *fmt, ...);
 void cuda_check(cudaError_t err, const char *what);
+// Sets the message returned by qg_last_error() on this thread.
+void set_last_error(const std::string &msg);
 #define QG_CUDA(call) ::qg::cuda_check((call), #call)
 
 // ---------------------------------------------------------------- kernels
