@@ -11,11 +11,18 @@ larger than the 129 MB L2, so no L2 flush is needed between steps.
 
 A step = reset the resident state to |0...0> and run the 900-gate circuit
 through the runtime plugin API (gates are queued, fused into shared-memory
-stages and launched at synchronize).  `value` = algorithmic bytes of the
-gate passes executed (one read + one write of every touched amplitude) per
-second of device time.  `e2e` = the same bytes per second of a step that
-also brings the circuit's outputs to the host through the plugin API: the
-full probability vector and 1e7 samples drawn from pre-drawn uniforms.
+stages and launched at synchronize).  `value` = gate-pass bytes per second of
+device time, where each gate counts the bytes the reference moves for it as a
+standalone pass (one read + one write of every amplitude it touches, the
+unfused sweep of qgate/simulator/src/DeviceProcPrimitives.cu:198-249); the
+same definition as the `--impl reference` arm, which runs those passes one by
+one.  Fused stages apply many gates per HBM pass, so `value` can exceed the
+HBM bandwidth; the bytes the engine actually moves, and the per-launch
+roofline of the dominant kernel, are reported beside it (`config`,
+`roofline`), as is the HBM efficiency of a single unfused gate pass.
+`e2e` = the same gate-pass bytes per second of a step that also brings the
+circuit's outputs to the host through the plugin API: the full probability
+vector and 1e7 samples drawn from pre-drawn uniforms.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -227,7 +234,13 @@ def run_gb300(args):
     dtype = np.float64 if args.dtype == 'c128' else np.float32
     ops = circuit(n, args.depth)
     gts = [(gate_type(nm, *a), t, list(c)) for nm, a, t, c in ops]
-    nat.set_fusion(args.tile)
+    unfused_bytes = gate_pass_bytes(n, ops, cs)
+    if args.tile == 0:
+        from qgate_gb300 import autotune
+        tuned = autotune.tune(n, dtype, ops, use_cache=not args.retune)
+    else:
+        nat.set_fusion(args.tile)
+        tuned = {'tile_lanes': args.tile}
 
     qs = rt.create_qubit_states(dtype)
     proc = qs.processor
@@ -271,7 +284,8 @@ def run_gb300(args):
         t = torch.tensor([dev_ms], dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_max = float(t[0])
-    value = moved * world / (t_max / 1e3) / 1e9
+    value = unfused_bytes * args.steps * world / (t_max / 1e3) / 1e9
+    hbm_actual = moved * world / (t_max / 1e3) / 1e9
     launches = sum(v[0] for v in timing.values())
 
     # roofline of the dominant kernel class
@@ -291,6 +305,9 @@ def run_gb300(args):
                 'frac': achieved / peak, 'peak_source': peak_kind,
                 'traffic': traffic, 'algorithmic_bytes_per_launch': alg,
                 'launches': dom_launches, 'avg_launch_ms': dom_ms / max(1, dom_launches)}
+
+    # HBM efficiency of single unfused gate passes (the reference's per-gate sweep)
+    single = single_gate_passes(nat, proc, qs, gts, n, cs, torch)
 
     # end to end through the plugin API with host buffers
     e2e = None
@@ -312,10 +329,15 @@ def run_gb300(args):
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': args.dtype, 'data': 'synthetic',
             'config': config_block(args, {
-                'fusion_tile_lanes': args.tile, 'passes_per_step': per_step_passes,
+                'fusion': {k: tuned.get(k) for k in ('tile_lanes', 'reg_lanes', 'cost_budget')},
+                'value_definition': 'unfused gate-pass bytes (each gate as its own read+write '
+                                    'sweep of the amplitudes it touches) per second',
+                'hbm_gbs_actual': hbm_actual,
+                'single_gate_pass': single,
+                'passes_per_step': per_step_passes,
                 'gates_per_step': stats['gates'] / args.steps,
                 'gate_pass_bytes_per_step': stats['bytes'] / args.steps,
-                'unfused_gate_pass_bytes_per_step': gate_pass_bytes(n, ops, cs),
+                'unfused_gate_pass_bytes_per_step': unfused_bytes,
                 'circuit_ms': t_max / args.steps,
                 'gates_per_s': stats['gates'] / args.steps / (t_max / args.steps / 1e3)}),
             'roofline': roofline,
@@ -329,6 +351,41 @@ def run_gb300(args):
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
+
+
+def single_gate_passes(nat, proc, qs, gts, n, cs, torch, count=8):
+    """Times `count` U3 gates of the circuit each as its own unfused pass
+    (fusion off) on the resident state: the per-pass HBM efficiency of the
+    single-gate kernel."""
+    g1 = [g for g in gts if not g[2]][:count]
+    stream = torch.cuda.ExternalStream(nat.stream_handle())
+    saved = None
+    try:
+        nat.set_fusion_params(nat.PREC_FP32 if cs == 8 else nat.PREC_FP64, 1, 4, 0)
+        saved = True
+        for gt, t, c in g1:
+            proc.apply_gate(gt, False, qs, t)
+        proc.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for gt, t, c in g1:
+            proc.apply_gate(gt, False, qs, t)
+        proc.synchronize()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / len(g1)
+    finally:
+        if saved:
+            from qgate_gb300 import autotune
+            cached = autotune._load().get(autotune._key(n, np.float32 if cs == 8 else np.float64))
+            if cached:
+                autotune.apply(cached)
+            else:
+                nat.set_fusion(0)
+    gbs = 2 * (1 << n) * cs / (ms / 1e3) / 1e9
+    peak, kind = measured_peak_hbm()
+    return {'kernel': 'k_pairs (one 2x2 gate per pass)', 'ms_per_pass': ms, 'gbs': gbs,
+            'frac_of_peak': gbs / peak, 'peak_source': kind}
 
 
 def run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2):
@@ -356,8 +413,8 @@ def run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2):
         e2e_step()
     dt = time.perf_counter() - t0
     stats = nat.gate_stats(reset=True)
-    moved = stats['bytes'] + (1 << n) * cs * args.e2e_steps
-    return {'value': moved / dt / 1e9, 'unit': 'GB/s',
+    unfused = gate_pass_bytes(n, ops, cs) * args.e2e_steps
+    return {'value': unfused / dt / 1e9, 'unit': 'GB/s',
             'h2d_bytes_per_step': args.samples * 8 + len(ops) * 64,
             'd2h_bytes_per_step': (1 << n) * (cs // 2) + args.samples * 8,
             'steps': args.e2e_steps, 'ms_per_step': dt / args.e2e_steps * 1e3,
@@ -374,7 +431,9 @@ def main():
     ap.add_argument('--qubits', type=int, default=30)
     ap.add_argument('--depth', type=int, default=20)
     ap.add_argument('--dtype', default='c64', choices=['c64', 'c128'])
-    ap.add_argument('--tile', type=int, default=0, help='fusion tile lanes (0 = default, 1 = off)')
+    ap.add_argument('--tile', type=int, default=0,
+                    help='fusion tile lanes (0 = autotuned, 1 = fusion off)')
+    ap.add_argument('--retune', action='store_true', help='ignore the autotuner cache')
     ap.add_argument('--samples', type=int, default=10_000_000)
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-e2e', action='store_true')

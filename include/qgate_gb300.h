@@ -140,6 +140,11 @@ int qg_qubit_processor_calc_norm(qg_handle proc, qg_handle qstates, double *out)
  * every gate is its own pass).  Pending gates are flushed at every
  * observation, join, measure or synchronize. */
 int qg_set_fusion(int max_tile_lanes);
+/* Extension: fusion parameters for one precision: lanes per shared-memory
+ * tile (1..14; complex128 at most 13), lanes held in each thread's registers
+ * by the register-resident stage kernel (3..5; complex128 at most 4), and a
+ * per-amplitude instruction budget that closes a stage early (0 = none). */
+int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budget);
 /* Extension: counters of the gate path since the last reset
  * {gates, passes, bytes_moved}. */
 int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset);
@@ -161,6 +166,45 @@ int qg_get_stream(uint64_t *stream);
  * (2^n_lanes complex values in the state's precision). */
 int qg_qubit_states_get_raw(qg_handle qstates, void *host, int64_t n);
 int qg_qubit_states_set_raw(qg_handle qstates, const void *host, int64_t n);
+
+/* ---- adjoint differentiation (extension) -------------------------------- */
+
+/* One gate of a parametrised circuit.  kind 0: fixed 2x2 gate `mat`;
+ * kind 1: rotation exp(-i coef theta G) with G = X/Y/Z (axis 1/2/3) on
+ * `target` and theta = params[param] (Rx/Ry/Rz: coef 1/2; ExpiZ: coef -1).
+ * Up to 4 controls. */
+typedef struct {
+    int kind;
+    int target;
+    int n_controls;
+    int controls[4];
+    int axis;
+    int param;
+    double coef;
+    double mat[8];
+} qg_circuit_op;
+
+/* One term coef * P of a Pauli-sum observable: X or Y on x_mask lanes, Z or Y
+ * on z_mask lanes (Y where both are set). */
+typedef struct {
+    double coef;
+    uint64_t x_mask;
+    uint64_t z_mask;
+} qg_pauli_term;
+
+/* Extension (the reference has no differentiation path).  For each of
+ * `batch` parameter vectors (params: batch x n_params, row-major) runs the
+ * circuit from |0...0> and returns E_b = <psi|H|psi> (FP64 accumulation) and,
+ * if gradients != NULL, dE_b/dparams (batch x n_params) by the adjoint
+ * method: one forward sweep, then a reverse sweep that un-applies every gate
+ * from psi and lambda = H psi while accumulating 2 coef Im<lambda|G|psi> per
+ * rotation.  With checkpoint_every = K > 0, psi is stored after every K gates
+ * on the way forward and restored there on the way back, which bounds the
+ * rounding drift of the un-applied complex64 state.  Blocking. */
+int qg_adjoint_expectation(int prec, int n_qubits, const qg_circuit_op *ops, int n_ops,
+                           const double *params, int n_params, int batch,
+                           const qg_pauli_term *terms, int n_terms, int checkpoint_every,
+                           double *expectations, double *gradients);
 
 /* ---- allocation-free variant ------------------------------------------- */
 

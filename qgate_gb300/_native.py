@@ -53,6 +53,7 @@ SIGNATURES = {
     'qg_qubit_processor_calc_pauli_expectation': [_h, _h, _u64, _u64, _dp],
     'qg_qubit_processor_calc_norm': [_h, _h, _dp],
     'qg_set_fusion': [_i],
+    'qg_set_fusion_params': [_i, _i, _i, _i],
     'qg_gate_stats': [_i64p, _i64p, _i64p, _i],
     'qg_timing_enable': [_i],
     'qg_timing_read': [ctypes.c_char_p, _i64p, _dp, _i],
@@ -62,6 +63,7 @@ SIGNATURES = {
     'qg_qubit_states_set_raw': [_h, _vp, _i64],
     'qg_gate_matrix': [ctypes.c_char_p, _dp, _i, _i, _dp],
     'qg_calc_probability_noalloc': [_i, _vp, _i, _i, _vp, _u64],
+    'qg_adjoint_expectation': [_i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _vp, _vp],
     'qg_qubits_states_getter_new': [_i, _hp],
     'qg_qubits_states_getter_delete': [_h],
     'qg_qubits_states_getter_get_states': [_h, _vp, _i64, _i, _ip, _ip, _hp, _i, _u64, _i,
@@ -141,6 +143,10 @@ def gate_matrix(name, args=(), adjoint=False):
 
 def set_fusion(max_tile_lanes):
     call('qg_set_fusion', int(max_tile_lanes))
+
+
+def set_fusion_params(prec, tile_lanes, reg_lanes, cost_budget=0):
+    call('qg_set_fusion_params', int(prec), int(tile_lanes), int(reg_lanes), int(cost_budget))
 
 
 def gate_stats(reset=False):

@@ -1,0 +1,104 @@
+"""Autotuner for the fused-stage kernel's tile shape.
+
+The fusion planner packs gates into shared-memory tiles of `tile_lanes`
+lanes, run by the register-resident stage kernel with `reg_lanes` lanes per
+thread's registers, and closes a stage when its estimated per-amplitude
+instruction count passes `cost_budget`.  Which shape is fastest depends on
+the state size, the precision and the gate mix, so this module times a
+candidate grid on a caller-supplied circuit and keeps the best shape per
+(device, lanes, precision) in a JSON cache next to the package.
+
+    from qgate_gb300 import autotune
+    best = autotune.tune(n_lanes, np.float32, ops)   # ops: [(name, args, target, controls)]
+    autotune.apply(best)
+"""
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _native as nat
+from .circuit import gate_type
+
+CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), '_tuning.json')
+
+# (tile_lanes, reg_lanes, cost_budget)
+CANDIDATES = {
+    np.float32: [(10, 4, 0), (11, 4, 0), (11, 5, 0), (12, 4, 0), (12, 5, 0), (13, 4, 0),
+                 (13, 5, 0), (12, 4, 130), (11, 4, 130)],
+    np.float64: [(10, 4, 0), (11, 4, 0), (12, 4, 0), (13, 4, 0), (11, 3, 0)],
+}
+
+
+def _key(n_lanes, dtype):
+    info = nat.device_info()
+    return '%d.%d/%d/%s' % (info['cc_major'], info['cc_minor'], n_lanes,
+                            'c128' if dtype == np.float64 else 'c64')
+
+
+def _load():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _prec(dtype):
+    return nat.PREC_FP64 if dtype == np.float64 else nat.PREC_FP32
+
+
+def apply(best):
+    nat.set_fusion_params(best['prec'], best['tile_lanes'], best['reg_lanes'],
+                          best['cost_budget'])
+
+
+def tune(n_lanes, dtype, ops, repeats=2, use_cache=True, candidates=None):
+    """Times every candidate shape on `ops` applied to a resident 2^n_lanes
+    state and returns the fastest as a dict (also cached on disk)."""
+    from . import gb300runtime as rt
+    key = _key(n_lanes, dtype)
+    cache = _load()
+    if use_cache and key in cache and candidates is None:
+        return cache[key]
+    gts = [(gate_type(nm, *a), t, list(c)) for nm, a, t, c in ops]
+    qs = rt.create_qubit_states(dtype)
+    proc = qs.processor
+    proc.initialize_qubit_states(qs, n_lanes)
+
+    def run():
+        proc.reset_qubit_states(qs)
+        for gt, t, c in gts:
+            if c:
+                proc.apply_controlled_gate(gt, False, qs, c, t)
+            else:
+                proc.apply_gate(gt, False, qs, t)
+        proc.synchronize()
+
+    prec = _prec(dtype)
+    results = []
+    for tile, rl, budget in (candidates or CANDIDATES[dtype]):
+        if tile > n_lanes:
+            continue
+        nat.set_fusion_params(prec, tile, rl, budget)
+        run()
+        t0 = time.perf_counter()
+        for _ in range(repeats):
+            run()
+        dt = (time.perf_counter() - t0) / repeats
+        results.append((dt, tile, rl, budget))
+    qs.delete()
+    results.sort()
+    dt, tile, rl, budget = results[0]
+    best = {'prec': prec, 'tile_lanes': tile, 'reg_lanes': rl, 'cost_budget': budget,
+            'circuit_ms': dt * 1e3,
+            'table': [[r[1], r[2], r[3], r[0] * 1e3] for r in results]}
+    cache[key] = best
+    try:
+        with open(CACHE, 'w') as f:
+            json.dump(cache, f, indent=1)
+    except OSError:
+        pass
+    apply(best)
+    return best

@@ -147,7 +147,12 @@ struct Device {
     static constexpr size_t kStageBytes = 64ull << 20;
     void *h_stage[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
-    int tile_lanes[3] = {0, 13, 12};  // indexed by prec: [1] fp64, [2] fp32
+    // Fusion parameters, indexed by prec ([1] fp64, [2] fp32): lanes per
+    // shared-memory tile, lanes per thread's registers, per-amplitude cost
+    // budget of a stage (0 = unlimited).
+    int tile_lanes[3] = {0, 12, 13};
+    int reg_lanes[3] = {0, 4, 4};
+    int cost_budget[3] = {0, 0, 0};
     long long n_gates = 0, n_passes = 0, n_bytes = 0;
     // Per-kernel-class launch timing with CUDA events on the engine's stream.
     bool timing = false;
@@ -192,6 +197,10 @@ static Device &dev() {
     QG_CUDA(cudaSetDevice(g_dev.dev));
     return g_dev;
 }
+
+cudaStream_t engine_stream() { return dev().stream; }
+void *engine_alloc(size_t bytes) { return dev().arena.alloc(bytes); }
+void engine_free(void *p) { g_dev.arena.release(p); }
 
 template <class T> static T *lookup(std::unordered_set<T *> &set, qg_handle h, const char *what) {
     T *p = reinterpret_cast<T *>(h);
@@ -285,27 +294,43 @@ static unsigned long long gate_qmask(const PendingGate &g) {
     return q;
 }
 
-static void run_stage(Device &d, States *s, unsigned long long S,
-                      const std::vector<const PendingGate *> &gates) {
+static bool is_diag(const Mat2 &m) {
+    return m.v[2] == 0. && m.v[3] == 0. && m.v[4] == 0. && m.v[5] == 0.;
+}
+
+struct TileLanes {
+    std::vector<int> lanes;  // global lanes of the tile, ascending
+    int local_of[64];
+    int lowrun;
+};
+
+static TileLanes tile_lanes_of(unsigned long long S, int n) {
+    TileLanes tl;
+    for (int q = 0; q < n; ++q)
+        if (S & (1ULL << q)) tl.lanes.push_back(q);
+    for (int i = 0; i < 64; ++i) tl.local_of[i] = -1;
+    for (int i = 0; i < (int)tl.lanes.size(); ++i) tl.local_of[tl.lanes[i]] = i;
+    tl.lowrun = 0;
+    while (tl.lowrun < (int)tl.lanes.size() && tl.lanes[tl.lowrun] == tl.lowrun) ++tl.lowrun;
+    return tl;
+}
+
+// Shared-memory stage (generic, any tile size): used for tiles too small for
+// the register-resident kernel.
+static void run_stage_smem(Device &d, States *s, unsigned long long S,
+                           const std::vector<const PendingGate *> &gates) {
     StageDesc sd;
     memset(&sd, 0, sizeof(sd));
     const int n = s->n_lanes;
-    std::vector<int> lanes;
-    for (int q = 0; q < n; ++q)
-        if (S & (1ULL << q)) lanes.push_back(q);
-    const int m = (int)lanes.size();
-    int local_of[64];
-    for (int i = 0; i < 64; ++i) local_of[i] = -1;
-    for (int i = 0; i < m; ++i) local_of[lanes[i]] = i;
+    TileLanes tl = tile_lanes_of(S, n);
+    const int m = (int)tl.lanes.size();
     sd.n = n;
     sd.m = m;
-    int lowrun = 0;
-    while (lowrun < m && lanes[lowrun] == lowrun) ++lowrun;
-    sd.lowrun = lowrun;
-    sd.nhi = m - lowrun;
-    for (int j = 0; j < sd.nhi; ++j) sd.hi_pos[j] = lanes[lowrun + j];
+    sd.lowrun = tl.lowrun;
+    sd.nhi = m - tl.lowrun;
+    for (int j = 0; j < sd.nhi; ++j) sd.hi_pos[j] = tl.lanes[tl.lowrun + j];
     sd.nins = m < n ? m : 0;
-    for (int j = 0; j < sd.nins; ++j) sd.ins_pos[j] = lanes[j];
+    for (int j = 0; j < sd.nins; ++j) sd.ins_pos[j] = tl.lanes[j];
     sd.ngates = (int)gates.size();
     for (int gi = 0; gi < sd.ngates; ++gi) {
         const PendingGate &g = *gates[gi];
@@ -313,15 +338,15 @@ static void run_stage(Device &d, States *s, unsigned long long S,
         std::vector<int> pos;
         unsigned cmask = 0;
         for (int c : g.controls) {
-            pos.push_back(local_of[c]);
-            cmask |= 1u << local_of[c];
+            pos.push_back(tl.local_of[c]);
+            cmask |= 1u << tl.local_of[c];
         }
-        pos.push_back(local_of[g.target]);
+        pos.push_back(tl.local_of[g.target]);
         std::sort(pos.begin(), pos.end());
         G.npos = (int)pos.size();
         for (int i = 0; i < G.npos; ++i) G.pos[i] = (signed char)pos[i];
         G.cmask = cmask;
-        G.tbit = 1u << local_of[g.target];
+        G.tbit = 1u << tl.local_of[g.target];
         G.diag = g.diag ? 1 : 0;
         memcpy(G.m, g.m.v, sizeof(G.m));
     }
@@ -330,31 +355,231 @@ static void run_stage(Device &d, States *s, unsigned long long S,
     d.n_bytes += 2 * ((long long)1 << n) * (long long)complex_size(s->prec);
 }
 
+static bool is_x(const Mat2 &m) {
+    static const double x[8] = {0., 0., 1., 0., 1., 0., 0., 0.};
+    for (int i = 0; i < 8; ++i)
+        if (m.v[i] != x[i]) return false;
+    return true;
+}
+
+// Builds the register program of one stage: walks the gates in order and
+// keeps the targets of dense gates in the register set, inserting a
+// shared-memory transpose (to the next rl distinct targets) when a target is
+// not resident.  Diagonal gates never need one.  Returns false if the program
+// does not fit the descriptor.
+template <class R>
+static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const TileLanes &tl,
+                            int n, int rl, RStageDesc<R> &d) {
+    const int m = (int)tl.lanes.size();
+    const int t = m - rl;
+    memset(&d, 0, sizeof(d));
+    d.n = n;
+    d.m = m;
+    d.rl = rl;
+    d.lowrun = tl.lowrun;
+    d.nhi = m - tl.lowrun;
+    for (int j = 0; j < d.nhi; ++j) d.hi_pos[j] = tl.lanes[tl.lowrun + j];
+    d.nins = m < n ? m : 0;
+    for (int j = 0; j < d.nins; ++j) d.ins_pos[j] = tl.lanes[j];
+    for (int i = 0; i < (1 << rl); ++i) {
+        long long off = 0;
+        for (int k = 0; k < rl; ++k)
+            if (i & (1 << k)) off |= 1LL << tl.lanes[t + k];
+        d.dep_hi[i] = off;
+    }
+    const int ng = (int)gates.size();
+    std::vector<int> tgt(ng), kind(ng);
+    std::vector<unsigned> cm(ng);
+    for (int i = 0; i < ng; ++i) {
+        const PendingGate &g = *gates[i];
+        tgt[i] = tl.local_of[g.target];
+        unsigned c = 0;
+        for (int q : g.controls) c |= 1u << tl.local_of[q];
+        cm[i] = c;
+        kind[i] = g.diag ? kOpDiagReg : (is_x(g.m) ? kOpSwapX : kOpGate);
+    }
+    int nsets = 0;
+    std::vector<int> RB;
+    auto upcoming = [&](int from) {
+        std::vector<int> out;
+        for (int i = from; i < ng && (int)out.size() < rl; ++i) {
+            if (kind[i] == kOpDiagReg) continue;
+            if (std::find(out.begin(), out.end(), tgt[i]) == out.end()) out.push_back(tgt[i]);
+        }
+        return out;
+    };
+    auto emit_set = [&](std::vector<int> want) -> bool {
+        for (int b : RB)
+            if ((int)want.size() < rl && std::find(want.begin(), want.end(), b) == want.end())
+                want.push_back(b);
+        for (int b = 0; b < m && (int)want.size() < rl; ++b)
+            if (std::find(want.begin(), want.end(), b) == want.end()) want.push_back(b);
+        if (nsets >= kMaxRegSets || d.nops >= kMaxRegOps) return false;
+        unsigned mask = 0;
+        for (int k = 0; k < rl; ++k) {
+            d.rb[nsets][k] = (unsigned char)want[k];
+            mask |= 1u << want[k];
+        }
+        d.tbmask[nsets] = (unsigned short)(((1u << m) - 1) & ~mask);
+        RegOp<R> &o = d.ops[d.nops++];
+        o.kind = kOpTranspose;
+        o.reg = (unsigned char)nsets++;
+        RB = want;
+        return true;
+    };
+    if (!emit_set(upcoming(0))) return false;
+    for (int i = 0; i < ng; ++i) {
+        auto pos_in = [&](int b) {
+            for (int k = 0; k < rl; ++k)
+                if (RB[k] == b) return k;
+            return -1;
+        };
+        int k = pos_in(tgt[i]);
+        int kd = kind[i];
+        if (kd != kOpDiagReg && k < 0) {
+            if (!emit_set(upcoming(i))) return false;
+            k = pos_in(tgt[i]);
+        }
+        if (d.nops >= kMaxRegOps) return false;
+        RegOp<R> &o = d.ops[d.nops++];
+        unsigned rbmask = 0;
+        for (int b : RB) rbmask |= 1u << b;
+        unsigned jm = 0;
+        for (int kk = 0; kk < rl; ++kk)
+            if (cm[i] & (1u << RB[kk])) jm |= 1u << kk;
+        o.jmask = (unsigned short)jm;
+        o.tmask = cm[i] & ~rbmask;
+        if (kd == kOpDiagReg && k < 0) {
+            o.kind = kOpDiagThread;
+            o.tbit = 1u << tgt[i];
+            o.reg = 0;
+        } else {
+            o.kind = (unsigned char)kd;
+            o.reg = (unsigned char)k;
+        }
+        for (int v = 0; v < 8; ++v) o.m[v] = (R)gates[i]->m.v[v];
+    }
+    return true;
+}
+
+static void run_stage(Device &d, States *s, unsigned long long S,
+                      const std::vector<const PendingGate *> &gates) {
+    const int n = s->n_lanes;
+    TileLanes tl = tile_lanes_of(S, n);
+    const int m = (int)tl.lanes.size();
+    // Valid shapes: 32..512 threads (256 with 5 register lanes), 3..5
+    // register lanes (complex128 at most 4).
+    const int max_rl = s->prec == kFP64 ? 4 : 5;
+    auto max_t = [](int r) { return r >= 5 ? 8 : 9; };
+    int rl = std::min(d.reg_lanes[s->prec], max_rl);
+    while (rl < max_rl && m - rl > max_t(rl)) ++rl;
+    while (rl > 3 && m - rl < 5) --rl;
+    if (m - rl > max_t(rl) || m - rl < 5) {
+        run_stage_smem(d, s, S, gates);
+        return;
+    }
+    bool ok;
+    if (s->prec == kFP32) {
+        static RStageDesc<float> desc;
+        ok = schedule_rstage(gates, tl, n, rl, desc);
+        if (ok) timed(d, "stage", [&] { launch_rstage_f32(s->d, desc, d.stream); });
+    } else {
+        static RStageDesc<double> desc;
+        ok = schedule_rstage(gates, tl, n, rl, desc);
+        if (ok) timed(d, "stage", [&] { launch_rstage_f64(s->d, desc, d.stream); });
+    }
+    if (!ok) {
+        // Program too long for one descriptor: split the stage.
+        size_t h = gates.size() / 2;
+        std::vector<const PendingGate *> a(gates.begin(), gates.begin() + h),
+            b(gates.begin() + h, gates.end());
+        run_stage(d, s, S, a);
+        run_stage(d, s, S, b);
+        return;
+    }
+    d.n_passes += 1;
+    d.n_bytes += 2 * ((long long)1 << n) * (long long)complex_size(s->prec);
+}
+
+static void mat_mul(const Mat2 &a, const Mat2 &b, Mat2 &out) {  // out = a * b
+    for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < 2; ++c) {
+            double re = 0., im = 0.;
+            for (int k = 0; k < 2; ++k) {
+                double ar = a.v[2 * (2 * r + k)], ai = a.v[2 * (2 * r + k) + 1];
+                double br = b.v[2 * (2 * k + c)], bi = b.v[2 * (2 * k + c) + 1];
+                re += ar * br - ai * bi;
+                im += ar * bi + ai * br;
+            }
+            out.v[2 * (2 * r + c)] = re;
+            out.v[2 * (2 * r + c) + 1] = im;
+        }
+}
+
+// Merges each uncontrolled single-lane gate into the previous gate on its lane
+// when that gate is also uncontrolled on the same lane (no gate in between
+// touches the lane), so the pair costs one 2x2 update.
+static void merge_runs(std::vector<PendingGate> &gates) {
+    std::vector<PendingGate> out;
+    out.reserve(gates.size());
+    int last[64];
+    for (int i = 0; i < 64; ++i) last[i] = -1;
+    for (auto &g : gates) {
+        int prev = last[g.target];
+        if (g.controls.empty() && prev >= 0 && out[prev].controls.empty() &&
+            out[prev].target == g.target) {
+            Mat2 prod;
+            mat_mul(g.m, out[prev].m, prod);
+            out[prev].m = prod;
+            out[prev].diag = is_diag(prod);
+            continue;
+        }
+        out.push_back(g);
+        int idx = (int)out.size() - 1;
+        last[g.target] = idx;
+        for (int c : g.controls) last[c] = idx;
+    }
+    gates.swap(out);
+}
+
+// Per-amplitude instruction estimate of a gate inside a register stage.
+static int gate_cost(const PendingGate &g) {
+    if (g.diag) return 4;
+    if (is_x(g.m)) return 2;
+    return 9;
+}
+
 // Fusion planner.  Walks the pending gates in order and packs them into
 // stages whose lane set S has at most M lanes; a gate that does not fit, or
 // that touches a lane of an earlier deferred gate, is deferred to the next
 // stage (it then commutes with everything moved ahead of it, because their
 // lane sets are disjoint).  The lowest lanes are always in S so that each
-// tile is made of >= 128-byte contiguous runs.
+// tile is made of >= 128-byte contiguous runs.  A per-amplitude cost budget
+// closes a stage before its arithmetic outgrows its HBM time.
 static void flush(States *s) {
     if (s->pending.empty()) return;
     Device &d = dev();
     const int n = s->n_lanes;
     int M = d.tile_lanes[s->prec];
-    std::vector<const PendingGate *> remaining;
-    for (auto &g : s->pending) remaining.push_back(&g);
     if (M <= 1) {
-        for (auto *g : remaining) run_single_gate(d, s, *g);
+        for (auto &g : s->pending) run_single_gate(d, s, g);
         s->pending.clear();
         return;
     }
+    merge_runs(s->pending);
+    std::vector<const PendingGate *> remaining;
+    for (auto &g : s->pending) remaining.push_back(&g);
     if (M > kMaxTileLanes) M = kMaxTileLanes;
+    if (s->prec == kFP64 && M > 13) M = 13;
+    const int budget = d.cost_budget[s->prec];
+    const int rl = d.reg_lanes[s->prec];
     const int low = std::min(n, s->prec == kFP32 ? 4 : 3);
     const unsigned long long all = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
     if (n <= M) M = n;
     const unsigned long long base = (n <= M) ? all : ((1ULL << low) - 1);
     while (!remaining.empty()) {
-        unsigned long long S = base, blocked = 0;
+        unsigned long long S = base, blocked = 0, dense_targets = 0;
+        int cost = 0;
         std::vector<const PendingGate *> chosen, deferred;
         // A gate wider than a tile runs on its own.
         if (__builtin_popcountll(gate_qmask(*remaining[0]) | base) > M) {
@@ -364,13 +589,20 @@ static void flush(States *s) {
         }
         for (auto *g : remaining) {
             unsigned long long q = gate_qmask(*g);
-            if ((q & blocked) || (int)chosen.size() >= kMaxStageGates ||
+            int c = gate_cost(*g);
+            unsigned long long dt = dense_targets;
+            if (!g->diag) dt |= 1ULL << g->target;
+            int est = cost + c + 7 * (int)((__builtin_popcountll(dt) + rl - 1) / rl);
+            bool over = budget > 0 && !chosen.empty() && est > budget;
+            if ((q & blocked) || (int)chosen.size() >= kMaxStageGates || over ||
                 __builtin_popcountll(S | q) > M) {
                 deferred.push_back(g);
                 blocked |= q;
                 continue;
             }
             S |= q;
+            cost += c;
+            dense_targets = dt;
             chosen.push_back(g);
         }
         if (chosen.size() == 1) {
@@ -394,9 +626,6 @@ static double read_result(Device &d, double *d_val) {
     return d.h_result[0];
 }
 
-static bool is_diag(const Mat2 &m) {
-    return m.v[2] == 0. && m.v[3] == 0. && m.v[4] == 0. && m.v[5] == 0.;
-}
 
 // ------------------------------------------------------------ transfers
 
@@ -933,10 +1162,27 @@ int qg_set_fusion(int max_tile_lanes) {
     if (max_tile_lanes == 0) {
         g_dev.tile_lanes[kFP32] = 13;
         g_dev.tile_lanes[kFP64] = 12;
+        g_dev.reg_lanes[kFP32] = 4;
+        g_dev.reg_lanes[kFP64] = 4;
+        g_dev.cost_budget[kFP32] = 0;
+        g_dev.cost_budget[kFP64] = 0;
     } else {
         g_dev.tile_lanes[kFP32] = max_tile_lanes;
         g_dev.tile_lanes[kFP64] = std::min(max_tile_lanes, 13);
     }
+    QG_END
+}
+
+int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budget) {
+    QG_BEGIN
+    check_prec(prec);
+    if (tile_lanes < 1 || tile_lanes > kMaxTileLanes) fail(QG_ERR_VALUE, "tile_lanes out of range.");
+    if (reg_lanes < 3 || reg_lanes > kMaxRegLanes) fail(QG_ERR_VALUE, "reg_lanes must be in [3, 5].");
+    if (cost_budget < 0) fail(QG_ERR_VALUE, "cost_budget must be >= 0.");
+    flush_all();
+    g_dev.tile_lanes[prec] = tile_lanes;
+    g_dev.reg_lanes[prec] = reg_lanes;
+    g_dev.cost_budget[prec] = cost_budget;
     QG_END
 }
 

@@ -8,10 +8,12 @@
 // reference has no fusion: every gate is one full-state launch
 // (qgate/simulator/src/DeviceProcPrimitives.cu:198-249).
 #include "qg_device.cuh"
+#include "qg_regstage.cuh"
 
 namespace qg {
 
 namespace {
+using namespace rs;
 
 // ------------------------------------------------------------ fused stage
 
@@ -93,6 +95,139 @@ k_stage(typename CT<R>::type *__restrict__ s, const __grid_constant__ StageDesc 
     }
 }
 
+// ------------------------------------------------------------ register-resident stage
+
+// One CTA per tile of 2^m amplitudes, 2^(m-rl) threads, 2^rl amplitudes per
+// thread.  The stage program (ops, register sets, global offsets) is first
+// copied from the kernel parameters to shared memory, so that every thread
+// reads it with broadcast vector loads instead of per-field constant-bank
+// loads.  Load (cp.async, coalesced, swizzled) -> run the program (register
+// gates, diagonal phases, shared-memory transposes) -> store.
+template <class R, int RL>
+__global__ void __launch_bounds__(RL >= 5 ? 256 : 512)
+k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDesc<R> d) {
+    typedef typename CT<R>::type C;
+    typedef RegOp<R> Op;
+    constexpr int NR = 1 << RL;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int m = d.m;
+    C *sm = (C *)smraw;
+    Op *sops = (Op *)(smraw + ((size_t)sizeof(C) << m));
+    long long *sdep = (long long *)(sops + d.nops);
+    unsigned *sset = (unsigned *)(sdep + NR);  // per set: rb lanes packed 5x5 bits, tbmask
+    const int t = m - RL;
+    const unsigned tid = threadIdx.x;
+    const unsigned T = blockDim.x;
+
+    {
+        const int4 *src = (const int4 *)d.ops;
+        int4 *dst = (int4 *)sops;
+        const int nvec = (int)(d.nops * sizeof(Op) / sizeof(int4));
+        for (int i = tid; i < nvec; i += T) dst[i] = src[i];
+        if (tid < (unsigned)NR) sdep[tid] = d.dep_hi[tid];
+        for (int i = tid; i < kMaxRegSets; i += T) {
+            unsigned packed = 0;
+            for (int k = 0; k < RL; ++k) packed |= (unsigned)d.rb[i][k] << (5 * k);
+            sset[2 * i] = packed;
+            sset[2 * i + 1] = d.tbmask[i];
+        }
+    }
+    const idx_t base = insert_zeros((idx_t)blockIdx.x, d.ins_pos, d.nins);
+    // Global offset of tile element tid (tile lanes 0..t-1).
+    const int lr = d.lowrun < t ? d.lowrun : t;
+    idx_t dt = (idx_t)(tid & ((1u << lr) - 1u));
+    for (int b = lr; b < t; ++b)
+        if (tid & (1u << b)) dt |= 1LL << d.hi_pos[b - d.lowrun];
+    const unsigned pt = Swz<R>::f(tid);
+    __syncthreads();
+
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+        unsigned slot = pt ^ Swz<R>::f((unsigned)i << t);
+        cp_async_elem(&sm[slot], &s[base | dt | sdep[i]]);
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+
+    C a[NR];
+    unsigned e0 = 0, P0 = 0;
+    unsigned q[RL];
+#pragma unroll
+    for (int k = 0; k < RL; ++k) q[k] = 0;
+
+    const int nops = d.nops;
+    for (int oi = 0; oi < nops; ++oi) {
+        const Op o = sops[oi];
+        if (o.kind == kOpTranspose) {
+            if (oi > 0) {
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+                __syncthreads();
+            }
+            const unsigned packed = sset[2 * o.reg];
+            e0 = pdep_sw(tid, sset[2 * o.reg + 1]);
+            P0 = Swz<R>::f(e0);
+#pragma unroll
+            for (int k = 0; k < RL; ++k) q[k] = Swz<R>::f(1u << ((packed >> (5 * k)) & 31u));
+#pragma unroll
+            for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
+            continue;
+        }
+        if ((e0 & o.tmask) != o.tmask) continue;
+        if (o.kind == kOpGate) {
+            MatR<R> mm;
+            mm.m00 = cmk<C>(o.m[0], o.m[1]);
+            mm.m01 = cmk<C>(o.m[2], o.m[3]);
+            mm.m10 = cmk<C>(o.m[4], o.m[5]);
+            mm.m11 = cmk<C>(o.m[6], o.m[7]);
+            QG_REG_DISPATCH(reg_gate, o.reg, a, mm, (unsigned)o.jmask);
+        } else if (o.kind == kOpSwapX) {
+            QG_REG_DISPATCH(reg_swap, o.reg, a, (unsigned)o.jmask);
+        } else if (o.kind == kOpDiagReg) {
+            C d0 = cmk<C>(o.m[0], o.m[1]), d1 = cmk<C>(o.m[6], o.m[7]);
+            QG_REG_DISPATCH(reg_diag, o.reg, a, d0, d1, (unsigned)o.jmask);
+        } else {  // kOpDiagThread
+            C ph = (e0 & o.tbit) ? cmk<C>(o.m[6], o.m[7]) : cmk<C>(o.m[0], o.m[1]);
+#pragma unroll
+            for (int j = 0; j < NR; ++j)
+                if ((j & o.jmask) == o.jmask) a[j] = cmul(ph, a[j]);
+        }
+    }
+
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+        unsigned slot = pt ^ Swz<R>::f((unsigned)i << t);
+        s[base | dt | sdep[i]] = sm[slot];
+    }
+}
+
+template <class R>
+void rstage_dispatch(void *state, const RStageDesc<R> &d, cudaStream_t stream) {
+    typedef typename CT<R>::type C;
+    size_t smem = ((size_t)1 << d.m) * sizeof(C) + (size_t)d.nops * sizeof(RegOp<R>) +
+                  sizeof(long long) * (1 << d.rl) + sizeof(unsigned) * 2 * kMaxRegSets;
+    idx_t tiles = (idx_t)1 << (d.n - d.m);
+    int threads = 1 << (d.m - d.rl);
+    if (threads < 32 || threads > (d.rl >= 5 ? 256 : 512))
+        fail(2, "register stage: bad tile shape m=%d rl=%d", d.m, d.rl);
+    auto launch = [&](auto kern) {
+        QG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<(unsigned)tiles, threads, smem, stream>>>((C *)state, d);
+    };
+    switch (d.rl) {
+    case 3: launch(k_rstage<R, 3>); break;
+    case 4: launch(k_rstage<R, 4>); break;
+    case 5: launch(k_rstage<R, 5>); break;
+    default: fail(2, "register stage: unsupported register lanes %d", d.rl);
+    }
+    QG_CUDA(cudaGetLastError());
+}
+
 }  // namespace
 
 void launch_stage(int prec, void *state, const StageDesc &d, cudaStream_t stream) {
@@ -110,6 +245,14 @@ void launch_stage(int prec, void *state, const StageDesc &d, cudaStream_t stream
         k_stage<double><<<(unsigned)tiles, threads, smem, stream>>>((double2 *)state, d);
     }
     QG_CUDA(cudaGetLastError());
+}
+
+void launch_rstage_f32(void *state, const RStageDesc<float> &d, cudaStream_t stream) {
+    rstage_dispatch<float>(state, d, stream);
+}
+
+void launch_rstage_f64(void *state, const RStageDesc<double> &d, cudaStream_t stream) {
+    rstage_dispatch<double>(state, d, stream);
 }
 
 }  // namespace qg

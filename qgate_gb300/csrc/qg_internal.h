@@ -80,6 +80,115 @@ struct StageDesc {
     StageGate gates[kMaxStageGates];
 };
 
+// Register-resident fused stage.  Each thread holds 2^rl amplitudes of the
+// tile in registers: those whose tile index differs only in the tile lanes of
+// the current register set.  Gates whose target is in the register set are
+// applied in registers; diagonal gates need no data movement at all; a
+// transpose (through shared memory) switches to another register set.
+constexpr int kMaxRegOps = 192;
+constexpr int kMaxRegSets = 64;
+constexpr int kMaxRegLanes = 5;
+
+enum RegOpKind {
+    kOpGate = 0,        // dense 2x2 on register bit `reg`
+    kOpSwapX = 1,       // X (swap) on register bit `reg`
+    kOpDiagReg = 2,     // diagonal on register bit `reg`
+    kOpDiagThread = 3,  // diagonal whose target is a thread lane (tile mask `tbit`)
+    kOpTranspose = 4    // switch to register set `reg`
+};
+
+// 48 bytes (complex64) / 80 bytes (complex128): a whole number of 16-byte
+// vectors, so a stage program copies to shared memory as int4s.
+template <class R> struct alignas(16) RegOp {
+    unsigned char kind;
+    unsigned char reg;
+    unsigned short jmask;  // controls among register-index bits
+    unsigned tmask;        // controls among thread lanes (tile-lane mask)
+    unsigned tbit;         // kOpDiagThread: the target's tile-lane mask
+    unsigned pad;
+    R m[8];                // row-major 2x2 matrix, interleaved re/im
+};
+static_assert(sizeof(RegOp<float>) == 48, "RegOp<float> layout");
+static_assert(sizeof(RegOp<double>) == 80, "RegOp<double> layout");
+
+template <class R> struct RStageDesc {
+    int n, m, rl;              // lanes of the state, tile lanes, register lanes
+    int lowrun, nhi;
+    int hi_pos[kMaxTileLanes];
+    int nins;
+    int ins_pos[kMaxTileLanes];
+    long long dep_hi[1 << kMaxRegLanes];  // global offset of tile element (i << (m - rl))
+    int nops;
+    unsigned char rb[kMaxRegSets][kMaxRegLanes];  // register set -> tile lanes
+    unsigned short tbmask[kMaxRegSets];           // its complement (thread lanes)
+    RegOp<R> ops[kMaxRegOps];                     // 16-byte aligned
+};
+
+void launch_rstage_f32(void *state, const RStageDesc<float> &d, cudaStream_t stream);
+void launch_rstage_f64(void *state, const RStageDesc<double> &d, cudaStream_t stream);
+
+// ---------------------------------------------------------------- adjoint
+
+// One op of a batched stage program (forward apply, or backward un-apply with
+// gradient partials).  Matrices live in a per-batch-element table in device
+// memory (rotation matrices differ per parameter vector); `mat` indexes it.
+struct AdjOp {
+    unsigned char kind;   // RegOpKind
+    unsigned char reg;
+    unsigned short jmask;
+    unsigned tmask;
+    unsigned tbit;
+    unsigned short mat;   // matrix slot
+    unsigned char gaxis;  // 0: no gradient; 1/2/3: generator X/Y/Z of a rotation
+    unsigned char gslot;  // gradient slot within the stage
+};
+static_assert(sizeof(AdjOp) == 16, "AdjOp layout");
+
+constexpr int kMaxAdjOps = 256;
+constexpr int kMaxAdjSlots = 128;
+
+struct AdjStageDesc {
+    int n, m, rl;
+    int lowrun, nhi;
+    int hi_pos[kMaxTileLanes];
+    int nins;
+    int ins_pos[kMaxTileLanes];
+    long long dep_hi[1 << kMaxRegLanes];
+    int nops, nmats, ngrads;
+    unsigned char rb[kMaxRegSets][kMaxRegLanes];
+    unsigned short tbmask[kMaxRegSets];
+    AdjOp ops[kMaxAdjOps];
+};
+
+// mode 0: apply ops to psi.  mode 1: for each op, first accumulate the
+// gradient term Im<lam|P1 G|psi> of its slot (if any), then apply the op's
+// (adjoint) matrix to both psi and lam.  mats: [batch][nmats][8] in the
+// state's precision; grad_partials: [batch][ngrads][tiles] in the state's
+// precision.  States of batch element b start at b * 2^n.
+void launch_adj_stage(int prec, int mode, void *psi, void *lam, const AdjStageDesc &d,
+                      const void *mats, void *grad_partials, int batch, cudaStream_t stream);
+// grad[b * n_params + param[s]] += scale[s] * sum_t partials[b][s][t]  (FP64)
+void launch_adj_grad_reduce(int prec, const void *partials, int batch, int nslots, idx_t tiles,
+                            const int *d_param, const double *d_scale, double *grad,
+                            int n_params, cudaStream_t stream);
+
+struct PauliTerm {
+    double coef;
+    unsigned long long x, z;
+};
+constexpr int kMaxPauliTerms = 256;
+// lam = sum_t coef_t P_t psi and e_partials[b][block] for E_b = Re<psi|lam>.
+void launch_pauli_sum_apply(int prec, const void *psi, void *lam, int n, int batch,
+                            const PauliTerm *terms, int nterms, double *e_partials,
+                            int blocks_per_batch, cudaStream_t stream);
+int pauli_sum_blocks();
+void launch_sum_rows(const double *partials, int rows, int cols, double *out, cudaStream_t stream);
+
+// Engine services for other translation units.
+cudaStream_t engine_stream();
+void *engine_alloc(size_t bytes);
+void engine_free(void *p);
+
 // Descriptor of a lane-permuted gather over a product of states.
 struct GatherDesc {
     int nqs;

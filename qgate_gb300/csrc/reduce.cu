@@ -40,6 +40,15 @@ template <class C> __device__ __forceinline__ double abs2d(C c) {
     return (double)c.x * (double)c.x + (double)c.y * (double)c.y;
 }
 
+// |c|^2 in the state's precision.  complex64 terms are formed and summed in
+// FP32 over a short unrolled run (kUnroll items) and only that partial is
+// added to the FP64 accumulator: GB300's FP64 rate is a small fraction of its
+// FP32 rate, and a per-element FP64 multiply-add would make these HBM sweeps
+// compute-bound.  The FP32 partial of a few terms carries a relative error of
+// a few 1e-8, below the precision of the complex64 amplitudes themselves;
+// the long accumulation is FP64.
+template <class C> __device__ __forceinline__ auto abs2r(C c) { return c.x * c.x + c.y * c.y; }
+
 // Pr(lane == 0): sum of |psi[i0]|^2 over the pair sweep's first members.
 template <class R>
 __global__ void __launch_bounds__(kRedThreads)
@@ -53,11 +62,13 @@ k_prob_scalar(const typename CT<R>::type *__restrict__ s, idx_t n_items, PairIdx
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u)
             v[u] = s[insert_zeros(k + u * stride, pi.pos, pi.npos) | (idx_t)pi.set_mask];
+        R part = 0;
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) acc += abs2d(v[u]);
+        for (int u = 0; u < kUnroll; ++u) part += abs2r(v[u]);
+        acc += (double)part;
     }
     for (; k < n_items; k += stride)
-        acc += abs2d(s[insert_zeros(k, pi.pos, pi.npos) | (idx_t)pi.set_mask]);
+        acc += (double)abs2r(s[insert_zeros(k, pi.pos, pi.npos) | (idx_t)pi.set_mask]);
     acc = block_sum(acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
@@ -73,21 +84,22 @@ k_prob_vec2_f32(const float4 *__restrict__ s, idx_t n_vec, PairIdx pi, double *p
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u)
             a[u] = s[(insert_zeros(2 * (v + u * stride), pi.pos, pi.npos) | (idx_t)pi.set_mask) >> 1];
+        float part = 0.f;
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u)
-            acc += (double)a[u].x * a[u].x + (double)a[u].y * a[u].y +
-                   (double)a[u].z * a[u].z + (double)a[u].w * a[u].w;
+            part += a[u].x * a[u].x + a[u].y * a[u].y + a[u].z * a[u].z + a[u].w * a[u].w;
+        acc += (double)part;
     }
     for (; v < n_vec; v += stride) {
         float4 a = s[(insert_zeros(2 * v, pi.pos, pi.npos) | (idx_t)pi.set_mask) >> 1];
-        acc += (double)a.x * a.x + (double)a.y * a.y + (double)a.z * a.z + (double)a.w * a.w;
+        acc += (double)(a.x * a.x + a.y * a.y + a.z * a.z + a.w * a.w);
     }
     acc = block_sum(acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
-__device__ __forceinline__ double parity_sign(idx_t b) {
-    return (__popcll((unsigned long long)b) & 1) ? -1. : 1.;
+template <class R> __device__ __forceinline__ R parity_sign_r(idx_t b) {
+    return (__popcll((unsigned long long)b) & 1) ? R(-1) : R(1);
 }
 
 // <psi|P|psi>, diagonal Pauli string (x_mask == 0).
@@ -97,37 +109,55 @@ k_pauli_diag(const typename CT<R>::type *__restrict__ s, idx_t n, unsigned long 
              double *partials) {
     double acc = 0.;
     const idx_t stride = (idx_t)gridDim.x * blockDim.x;
-    for (idx_t b = (idx_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += stride)
-        acc += parity_sign(b & (idx_t)z_mask) * abs2d(s[b]);
+    idx_t b = (idx_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; b + (kUnroll - 1) * stride < n; b += kUnroll * stride) {
+        typename CT<R>::type v[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) v[u] = s[b + u * stride];
+        R part = 0;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+            part += parity_sign_r<R>((b + u * stride) & (idx_t)z_mask) * abs2r(v[u]);
+        acc += (double)part;
+    }
+    for (; b < n; b += stride)
+        acc += (double)(parity_sign_r<R>(b & (idx_t)z_mask) * abs2r(s[b]));
     acc = block_sum(acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
 // <psi|P|psi> with x_mask != 0: pairs (b, b ^ x_mask), b with the highest
-// x bit clear; ny = number of Y factors (x & z).
+// x bit clear; ny = number of Y factors (x & z).  With w = conj(psi[b^x]) psi[b]
+// and s1, s2 the Z-signs of b and b^x, the pair contributes
+// Re(i^ny (s1 w + s2 conj(w))).
 template <class R>
 __global__ void __launch_bounds__(kRedThreads)
 k_pauli_pair(const typename CT<R>::type *__restrict__ s, idx_t n_items, int hbit,
              unsigned long long x_mask, unsigned long long z_mask, int ny, double *partials) {
     double acc = 0.;
     const idx_t stride = (idx_t)gridDim.x * blockDim.x;
-    for (idx_t k = (idx_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_items; k += stride) {
-        idx_t b = insert_zero(k, hbit);
+    idx_t k = (idx_t)blockIdx.x * blockDim.x + threadIdx.x;
+    auto term = [&](idx_t kk) -> R {
+        idx_t b = insert_zero(kk, hbit);
         idx_t b2 = b ^ (idx_t)x_mask;
         typename CT<R>::type p = s[b], q = s[b2];
-        // w = conj(q) * p
-        double wr = (double)q.x * p.x + (double)q.y * p.y;
-        double wi = (double)q.x * p.y - (double)q.y * p.x;
-        double s1 = parity_sign(b & (idx_t)z_mask), s2 = parity_sign(b2 & (idx_t)z_mask);
-        double t;
+        R wr = q.x * p.x + q.y * p.y;
+        R wi = q.x * p.y - q.y * p.x;
+        R s1 = parity_sign_r<R>(b & (idx_t)z_mask), s2 = parity_sign_r<R>(b2 & (idx_t)z_mask);
         switch (ny & 3) {
-        case 0: t = (s1 + s2) * wr; break;
-        case 1: t = -(s1 - s2) * wi; break;
-        case 2: t = -(s1 + s2) * wr; break;
-        default: t = (s1 - s2) * wi; break;
+        case 0: return (s1 + s2) * wr;
+        case 1: return -(s1 - s2) * wi;
+        case 2: return -(s1 + s2) * wr;
+        default: return (s1 - s2) * wi;
         }
-        acc += t;
+    };
+    for (; k + (kUnroll - 1) * stride < n_items; k += kUnroll * stride) {
+        R part = 0;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) part += term(k + u * stride);
+        acc += (double)part;
     }
+    for (; k < n_items; k += stride) acc += (double)term(k);
     acc = block_sum(acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
@@ -188,12 +218,12 @@ k_marginal(double *__restrict__ out, int n_lanes, idx_t hidden_per_group,
         for (idx_t c = c0; c < c0 + hidden_per_group; ++c) {
             idx_t ext = o | (c << n_lanes);
             if (identity) {
-                acc += abs2d(((const C *)g.ptr[0])[ext]);
+                acc += (double)abs2r(((const C *)g.ptr[0])[ext]);
             } else {
-                double v = 1.;
+                R v = 1;
                 for (int q = 0; q < g.nqs; ++q)
-                    v *= abs2d(((const C *)g.ptr[q])[to_local(g, q, ext)]);
-                acc += v;
+                    v *= abs2r(((const C *)g.ptr[q])[to_local(g, q, ext)]);
+                acc += (double)v;
             }
         }
         out[(idx_t)blockIdx.y * n_out + o] = acc;

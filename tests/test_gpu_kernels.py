@@ -80,6 +80,56 @@ def test_fused_stages_match_unfused(rt, dtype, tile):
         assert np.allclose(got, want, atol=tol), (n, tile, np.max(np.abs(got - want)))
 
 
+def _structured_circuits(rng, n):
+    """Dense random gates with up to 3 controls; a QFT-like ladder of
+    controlled phases (diagonal gates, many on thread lanes); CX-heavy layers
+    of U3 + random matchings; merged single-lane runs (Ry then Rz)."""
+    dense = random_ops(rng, n, 120, max_controls=3)
+    qft = []
+    for i in range(n):
+        qft.append(('g', 'H', (), False, i, ()))
+        for j in range(i + 1, n):
+            qft.append(('g', 'U1', (np.pi / (1 << (j - i)),), False, i, (j,)))
+    layers = []
+    for _ in range(3):
+        layers += [('g', 'U', tuple(rng.uniform(0, 6, 3)), False, q, ()) for q in range(n)]
+        p = rng.permutation(n)
+        layers += [('g', 'X', (), False, int(p[2 * k + 1]), (int(p[2 * k]),))
+                   for k in range(n // 2)]
+        layers += [('g', 'RY', (float(rng.uniform(-3, 3)),), False, q, ()) for q in range(n)]
+        layers += [('g', 'RZ', (float(rng.uniform(-3, 3)),), False, q, ()) for q in range(n)]
+    return [dense, qft, layers]
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_register_stage_shapes(rt, dtype):
+    """The register-resident stage kernel at every valid (tile lanes,
+    register lanes) shape, with and without a cost budget, on dense,
+    diagonal-heavy and CX-heavy circuits (n = 16, so tiles < state)."""
+    from qgate_gb300 import _native as nat
+    prec = nat.PREC_FP64 if dtype == np.float64 else nat.PREC_FP32
+    rng = np.random.default_rng(42)
+    n = 16
+    circuits = _structured_circuits(rng, n)
+    wants = [sv.run_ops(n, ops, np.complex128) for ops in circuits]
+    rls = (3, 4) if dtype == np.float64 else (3, 4, 5)
+    tol = 1e-11 if dtype == np.float64 else 1e-5
+    try:
+        for tile in (6, 8, 9, 10, 11, 12, 13):
+            for rl in rls:
+                for budget in (0, 40):
+                    nat.set_fusion_params(prec, tile, rl, budget)
+                    for ops, want in zip(circuits, wants):
+                        qs = new_state(rt, n, dtype)
+                        apply_ops(qs, ops)
+                        got = qs.get_raw()
+                        err = np.max(np.abs(got - want))
+                        assert err < tol, (tile, rl, budget, err)
+                        qs.delete()
+    finally:
+        nat.set_fusion(0)
+
+
 @pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
 def test_random_circuit_20q_fidelity(rt, dtype):
     """20 qubits, U3 layers + CX matchings (the 30-qubit benchmark circuit's
