@@ -314,6 +314,11 @@ def run_gb300(args):
     if not args.no_e2e and rank == 0:
         e2e = run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2)
 
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        qs.delete()
+        adjoint = run_adjoint(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         gbs, done, dt, thr = cpu_port_gate_rate(n, ops, cs, args.cpu_seconds)
@@ -341,6 +346,7 @@ def run_gb300(args):
                 'circuit_ms': t_max / args.steps,
                 'gates_per_s': stats['gates'] / args.steps / (t_max / args.steps / 1e3)}),
             'roofline': roofline,
+            'adjoint': adjoint,
             'cpu_baseline': cpu,
             'e2e': e2e,
             'gpu_launches': launches,
@@ -386,6 +392,38 @@ def single_gate_passes(nat, proc, qs, gts, n, cs, torch, count=8):
     peak, kind = measured_peak_hbm()
     return {'kernel': 'k_pairs (one 2x2 gate per pass)', 'ms_per_pass': ms, 'gbs': gbs,
             'frac_of_peak': gbs / peak, 'peak_source': kind}
+
+
+def run_adjoint(args):
+    """Adjoint gradients of the 24-qubit hardware-efficient ansatz (12 layers
+    of Ry, Rz on every qubit + CX ring, 576 parameters uniform(-pi, pi) from
+    default_rng(30), batch of 64 vectors) for the transverse-field Ising chain
+    H = -sum Z_i Z_{i+1} - 0.7 sum X_i, complex64 (checkpoints every 3 layers)
+    and complex128; gradient vectors per second and the complex64 error
+    against the complex128 gradients."""
+    from qgate_gb300.adjoint import expectation_and_gradient, hardware_efficient_ansatz, PauliSum
+    n, layers, B = args.adj_qubits, 12, args.adj_batch
+    c = hardware_efficient_ansatz(n, layers)
+    H = PauliSum.ising_chain(n)
+    params = np.random.default_rng(30).uniform(-math.pi, math.pi, (B, c.n_params))
+    out = {'workload': '%d qubits, %d layers (Ry, Rz on every qubit + CX ring), %d parameters, '
+                       'batch %d, H = -sum Z_i Z_i+1 - 0.7 sum X_i (open chain)'
+                       % (n, layers, c.n_params, B)}
+    res = {}
+    for name, dt, ck in (('fp32', np.float32, 3 * 3 * n), ('fp64', np.float64, 0)):
+        E, G = expectation_and_gradient(c, params[:1], H, dt, ck)  # warm-up
+        t0 = time.perf_counter()
+        for _ in range(args.adj_steps):
+            E, G = expectation_and_gradient(c, params, H, dt, ck)
+        dtm = (time.perf_counter() - t0) / args.adj_steps
+        res[name] = (E, G)
+        out[name + '_grads_per_s'] = B / dtm
+        out[name + '_ms_per_batch'] = dtm * 1e3
+    out['speedup_fp32_vs_fp64'] = out['fp32_grads_per_s'] / out['fp64_grads_per_s']
+    out['max_grad_err_fp32_vs_fp64'] = float(np.max(np.abs(res['fp32'][1] - res['fp64'][1])))
+    out['max_energy_err_fp32_vs_fp64'] = float(np.max(np.abs(res['fp32'][0] - res['fp64'][0])))
+    out['checkpoint_every_gates_fp32'] = 3 * 3 * n
+    return out
 
 
 def run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2):
@@ -438,6 +476,10 @@ def main():
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-adjoint', action='store_true')
+    ap.add_argument('--adj-qubits', type=int, default=24)
+    ap.add_argument('--adj-batch', type=int, default=64)
+    ap.add_argument('--adj-steps', type=int, default=1)
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--ref-gates', type=int, default=12)
     args = ap.parse_args()
