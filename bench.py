@@ -129,16 +129,19 @@ def measured_peak_hbm():
 
 
 def stage_traffic_per_launch(n, cs):
-    """DRAM bytes per fused-stage launch from the committed ncu summary
-    (profiles/stage_traffic.json: bytes per amplitude measured on a smaller
-    state, scaled to 2^n amplitudes), or None."""
+    """DRAM bytes per fused-stage launch: bytes per amplitude from the ncu
+    capture recorded in profiles/stage_traffic.txt (a smaller state, same
+    kernel; traffic grows in proportion to the amplitudes), scaled to 2^n."""
+    key = 'c64' if cs == 8 else 'c128'
     try:
-        with open(os.path.join(ROOT, 'profiles', 'stage_traffic.json')) as f:
-            d = json.load(f)
-        key = 'c64' if cs == 8 else 'c128'
-        return float(d[key]['dram_bytes_per_amp']) * (1 << n)
-    except Exception:
-        return None
+        with open(os.path.join(ROOT, 'profiles', 'stage_traffic.txt')) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 3 and parts[0] == key and parts[1] == 'dram_bytes_per_amp':
+                    return float(parts[2]) * (1 << n)
+    except OSError:
+        pass
+    return None
 
 
 # ------------------------------------------------------------------ CPU legs
