@@ -317,6 +317,10 @@ def run_gb300(args):
     if not args.no_e2e and rank == 0:
         e2e = run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2)
 
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = run_batch(args, nat)
+
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         qs.delete()
@@ -350,6 +354,7 @@ def run_gb300(args):
                 'gates_per_s': stats['gates'] / args.steps / (t_max / args.steps / 1e3)}),
             'roofline': roofline,
             'adjoint': adjoint,
+            'batch': batch,
             'cpu_baseline': cpu,
             'e2e': e2e,
             'gpu_launches': launches,
@@ -429,6 +434,33 @@ def run_adjoint(args):
     return out
 
 
+def run_batch(args, nat):
+    """4096 hardware-efficient-ansatz circuits of uneven size (n ~ U{8..20},
+    depth ~ U{4..12}, Ry and Rz on every qubit then a CX ladder; default_rng(20)),
+    complex64, sum_i <Z_i> per circuit in FP64: circuits per second of the
+    call (host planning + one CUDA graph) and of the graph alone."""
+    from qgate_gb300.batch import hea_batch, pack, sum_z
+    circuits = hea_batch(count=args.batch_circuits, seed=20)
+    packed = pack(circuits)
+    sum_z(packed=packed)  # warm-up
+    nat.timing_all(reset=True)
+    nat.timing_enable(True)
+    t0 = time.perf_counter()
+    for _ in range(args.batch_steps):
+        out = sum_z(packed=packed)
+    dt = (time.perf_counter() - t0) / args.batch_steps
+    nat.timing_enable(False)
+    launches, gms = nat.timing_read('batch', reset=True)
+    gates = int(packed[1][-1])
+    amps = sum((1 << n) * len(ops) for n, ops in circuits)
+    return {'workload': '%d circuits, n ~ U{8..20}, depth ~ U{4..12}, Ry+Rz layers + CX ladder, '
+                        'sum_i <Z_i> per circuit' % len(circuits),
+            'gates': gates, 'circuits_per_s': len(circuits) / dt, 'ms_per_batch': dt * 1e3,
+            'graph_ms': gms / max(1, launches), 'circuits_per_s_graph':
+                len(circuits) / (gms / max(1, launches) / 1e3),
+            'amplitude_updates_per_s': amps / dt, 'checksum': float(np.sum(out))}
+
+
 def run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2):
     """Same metric through the plugin API with host buffers: circuit, full
     probability vector to host, pool + 1e7 samples from host uniforms."""
@@ -480,6 +512,9 @@ def main():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
+    ap.add_argument('--no-batch', action='store_true')
+    ap.add_argument('--batch-circuits', type=int, default=4096)
+    ap.add_argument('--batch-steps', type=int, default=3)
     ap.add_argument('--adj-qubits', type=int, default=24)
     ap.add_argument('--adj-batch', type=int, default=64)
     ap.add_argument('--adj-steps', type=int, default=1)

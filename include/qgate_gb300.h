@@ -151,7 +151,7 @@ int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset);
 
 /* Extension: per-kernel-class launch timing with CUDA events recorded on the
  * engine's stream around each launch (classes: stage, gate, multi, init,
- * prob, pauli, measure, join, gather, marginal, scan, search). */
+ * prob, pauli, measure, join, gather, marginal, scan, search, batch). */
 int qg_timing_enable(int on);
 int qg_timing_read(const char *kernel_class, int64_t *launches, double *total_ms, int reset);
 /* Extension: device facts {SMs, max opt-in shared memory per block, L2 bytes,
@@ -205,6 +205,17 @@ int qg_adjoint_expectation(int prec, int n_qubits, const qg_circuit_op *ops, int
                            const double *params, int n_params, int batch,
                            const qg_pauli_term *terms, int n_terms, int checkpoint_every,
                            double *expectations, double *gradients);
+
+/* Extension (the reference runs one circuit at a time).  Runs n_circuits
+ * independent circuits from |0...0> in complex64 and writes
+ * out[c] = sum_i <Z_i> (FP64) of each.  Circuit c has n_qubits[c] lanes
+ * (8..30) and the fixed gates (kind 0) gates[gate_offsets[c] ..
+ * gate_offsets[c+1]).  Circuits of up to 13 qubits run entirely inside one
+ * CTA's shared memory; larger ones advance one fused stage per round over a
+ * packed arena; the whole batch is recorded and launched as one CUDA graph.
+ * Blocking. */
+int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
+                   const qg_circuit_op *gates, double *out);
 
 /* ---- allocation-free variant ------------------------------------------- */
 

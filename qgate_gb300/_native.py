@@ -64,6 +64,7 @@ SIGNATURES = {
     'qg_gate_matrix': [ctypes.c_char_p, _dp, _i, _i, _dp],
     'qg_calc_probability_noalloc': [_i, _vp, _i, _i, _vp, _u64],
     'qg_adjoint_expectation': [_i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _vp, _vp],
+    'qg_batch_sum_z': [_i, _i, _vp, _vp, _vp, _vp],
     'qg_qubits_states_getter_new': [_i, _hp],
     'qg_qubits_states_getter_delete': [_h],
     'qg_qubits_states_getter_get_states': [_h, _vp, _i64, _i, _ip, _ip, _hp, _i, _u64, _i,
@@ -167,7 +168,7 @@ def timing_read(kernel_class, reset=False):
 
 
 KERNEL_CLASSES = ('stage', 'gate', 'multi', 'init', 'prob', 'pauli', 'measure', 'join',
-                  'gather', 'marginal', 'scan', 'search')
+                  'gather', 'marginal', 'scan', 'search', 'batch')
 
 
 def timing_all(reset=False):

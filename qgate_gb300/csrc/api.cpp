@@ -365,28 +365,15 @@ static bool is_x(const Mat2 &m) {
 // Builds the register program of one stage: walks the gates in order and
 // keeps the targets of dense gates in the register set, inserting a
 // shared-memory transpose (to the next rl distinct targets) when a target is
-// not resident.  Diagonal gates never need one.  Returns false if the program
-// does not fit the descriptor.
+// not resident.  Diagonal gates never need one.  `sets` receives, per
+// register set, its rl tile lanes.
 template <class R>
-static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const TileLanes &tl,
-                            int n, int rl, RStageDesc<R> &d) {
+static void build_program(const std::vector<const PendingGate *> &gates, const TileLanes &tl,
+                          int rl, std::vector<RegOp<R>> &ops,
+                          std::vector<std::vector<int>> &sets) {
     const int m = (int)tl.lanes.size();
-    const int t = m - rl;
-    memset(&d, 0, sizeof(d));
-    d.n = n;
-    d.m = m;
-    d.rl = rl;
-    d.lowrun = tl.lowrun;
-    d.nhi = m - tl.lowrun;
-    for (int j = 0; j < d.nhi; ++j) d.hi_pos[j] = tl.lanes[tl.lowrun + j];
-    d.nins = m < n ? m : 0;
-    for (int j = 0; j < d.nins; ++j) d.ins_pos[j] = tl.lanes[j];
-    for (int i = 0; i < (1 << rl); ++i) {
-        long long off = 0;
-        for (int k = 0; k < rl; ++k)
-            if (i & (1 << k)) off |= 1LL << tl.lanes[t + k];
-        d.dep_hi[i] = off;
-    }
+    ops.clear();
+    sets.clear();
     const int ng = (int)gates.size();
     std::vector<int> tgt(ng), kind(ng);
     std::vector<unsigned> cm(ng);
@@ -398,7 +385,6 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
         cm[i] = c;
         kind[i] = g.diag ? kOpDiagReg : (is_x(g.m) ? kOpSwapX : kOpGate);
     }
-    int nsets = 0;
     std::vector<int> RB;
     auto upcoming = [&](int from) {
         std::vector<int> out;
@@ -408,26 +394,21 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
         }
         return out;
     };
-    auto emit_set = [&](std::vector<int> want) -> bool {
+    auto emit_set = [&](std::vector<int> want) {
         for (int b : RB)
             if ((int)want.size() < rl && std::find(want.begin(), want.end(), b) == want.end())
                 want.push_back(b);
         for (int b = 0; b < m && (int)want.size() < rl; ++b)
             if (std::find(want.begin(), want.end(), b) == want.end()) want.push_back(b);
-        if (nsets >= kMaxRegSets || d.nops >= kMaxRegOps) return false;
-        unsigned mask = 0;
-        for (int k = 0; k < rl; ++k) {
-            d.rb[nsets][k] = (unsigned char)want[k];
-            mask |= 1u << want[k];
-        }
-        d.tbmask[nsets] = (unsigned short)(((1u << m) - 1) & ~mask);
-        RegOp<R> &o = d.ops[d.nops++];
+        RegOp<R> o;
+        memset(&o, 0, sizeof(o));
         o.kind = kOpTranspose;
-        o.reg = (unsigned char)nsets++;
+        o.reg = (unsigned char)std::min<size_t>(sets.size(), 255);
+        ops.push_back(o);
+        sets.push_back(want);
         RB = want;
-        return true;
     };
-    if (!emit_set(upcoming(0))) return false;
+    emit_set(upcoming(0));
     for (int i = 0; i < ng; ++i) {
         auto pos_in = [&](int b) {
             for (int k = 0; k < rl; ++k)
@@ -437,11 +418,11 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
         int k = pos_in(tgt[i]);
         int kd = kind[i];
         if (kd != kOpDiagReg && k < 0) {
-            if (!emit_set(upcoming(i))) return false;
+            emit_set(upcoming(i));
             k = pos_in(tgt[i]);
         }
-        if (d.nops >= kMaxRegOps) return false;
-        RegOp<R> &o = d.ops[d.nops++];
+        RegOp<R> o;
+        memset(&o, 0, sizeof(o));
         unsigned rbmask = 0;
         for (int b : RB) rbmask |= 1u << b;
         unsigned jm = 0;
@@ -458,6 +439,51 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
             o.reg = (unsigned char)k;
         }
         for (int v = 0; v < 8; ++v) o.m[v] = (R)gates[i]->m.v[v];
+        ops.push_back(o);
+    }
+}
+
+static void fill_tile_header(const TileLanes &tl, int n, int rl, int &lowrun, int &nhi, int *hi_pos,
+                             int &nins, int *ins_pos, long long *dep_hi) {
+    const int m = (int)tl.lanes.size();
+    const int t = m - rl;
+    lowrun = tl.lowrun;
+    nhi = m - tl.lowrun;
+    for (int j = 0; j < nhi; ++j) hi_pos[j] = tl.lanes[tl.lowrun + j];
+    nins = m < n ? m : 0;
+    for (int j = 0; j < nins; ++j) ins_pos[j] = tl.lanes[j];
+    for (int i = 0; i < (1 << rl); ++i) {
+        long long off = 0;
+        for (int k = 0; k < rl; ++k)
+            if (i & (1 << k)) off |= 1LL << tl.lanes[t + k];
+        dep_hi[i] = off;
+    }
+}
+
+// Register program of one stage in a kernel-parameter descriptor.  Returns
+// false if it does not fit.
+template <class R>
+static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const TileLanes &tl,
+                            int n, int rl, RStageDesc<R> &d) {
+    std::vector<RegOp<R>> ops;
+    std::vector<std::vector<int>> sets;
+    build_program<R>(gates, tl, rl, ops, sets);
+    if ((int)ops.size() > kMaxRegOps || (int)sets.size() > kMaxRegSets) return false;
+    const int m = (int)tl.lanes.size();
+    memset(&d, 0, sizeof(d));
+    d.n = n;
+    d.m = m;
+    d.rl = rl;
+    fill_tile_header(tl, n, rl, d.lowrun, d.nhi, d.hi_pos, d.nins, d.ins_pos, d.dep_hi);
+    d.nops = (int)ops.size();
+    for (int i = 0; i < d.nops; ++i) d.ops[i] = ops[i];
+    for (size_t si = 0; si < sets.size(); ++si) {
+        unsigned mask = 0;
+        for (int k = 0; k < rl; ++k) {
+            d.rb[si][k] = (unsigned char)sets[si][k];
+            mask |= 1u << sets[si][k];
+        }
+        d.tbmask[si] = (unsigned short)(((1u << m) - 1) & ~mask);
     }
     return true;
 }
@@ -1269,6 +1295,210 @@ int qg_device_info(int64_t *info, int n) {
 int qg_get_stream(uint64_t *stream) {
     QG_BEGIN
     *stream = (uint64_t)(uintptr_t)dev().stream;
+    QG_END
+}
+
+// Greedy stage packing of a gate list (the gate queue's planner, reusable).
+static std::vector<std::pair<unsigned long long, std::vector<const PendingGate *>>>
+plan_gate_stages(const std::vector<PendingGate> &gates, int n, int M, int low) {
+    std::vector<std::pair<unsigned long long, std::vector<const PendingGate *>>> out;
+    std::vector<const PendingGate *> remaining;
+    for (auto &g : gates) remaining.push_back(&g);
+    const unsigned long long all = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+    if (n <= M) M = n;
+    const unsigned long long base = (n <= M) ? all : ((1ULL << low) - 1);
+    while (!remaining.empty()) {
+        unsigned long long S = base, blocked = 0;
+        std::vector<const PendingGate *> chosen, deferred;
+        for (auto *g : remaining) {
+            unsigned long long q = gate_qmask(*g);
+            if ((q & blocked) || (int)chosen.size() >= kMaxStageGates ||
+                __builtin_popcountll(S | q) > M) {
+                deferred.push_back(g);
+                blocked |= q;
+                continue;
+            }
+            S |= q;
+            chosen.push_back(g);
+        }
+        if (chosen.empty()) fail(QG_ERR_VALUE, "gate wider than a tile.");
+        for (int q = 0; q < n && __builtin_popcountll(S) < M; ++q) S |= 1ULL << q;
+        out.emplace_back(S, chosen);
+        remaining.swap(deferred);
+    }
+    return out;
+}
+
+static void append_sets(const std::vector<std::vector<int>> &sets, int m, int rl,
+                        std::vector<unsigned> &sets_all) {
+    for (auto &st : sets) {
+        unsigned packed = 0, mask = 0;
+        for (int k = 0; k < rl; ++k) {
+            packed |= (unsigned)st[k] << (5 * k);
+            mask |= 1u << st[k];
+        }
+        sets_all.push_back(packed);
+        sets_all.push_back(((1u << m) - 1) & ~mask);
+    }
+}
+
+int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
+                   const qg_circuit_op *gates, double *out) {
+    QG_BEGIN
+    if (prec != kFP32) fail(QG_ERR_VALUE, "batched circuits run in complex64.");
+    if (n_circuits < 1) fail(QG_ERR_VALUE, "no circuits.");
+    Device &d = dev();
+    std::vector<RegOp<float>> ops_all;
+    std::vector<unsigned> sets_all;
+    std::vector<ResidentCircuit> res[14];
+    std::vector<BatchStage> stages;
+    std::vector<std::vector<int2>> rounds;
+    std::vector<long long> big_off;
+    std::vector<int> big_n, big_idx;
+    long long arena_elems = 0;
+    std::vector<RegOp<float>> prog;
+    std::vector<std::vector<int>> sets;
+    for (int c = 0; c < n_circuits; ++c) {
+        const int n = n_qubits[c];
+        if (n < 8 || n > 30) fail(QG_ERR_VALUE, "circuit %d: 8..30 qubits supported.", c);
+        std::vector<PendingGate> gl;
+        for (int64_t gi = gate_offsets[c]; gi < gate_offsets[c + 1]; ++gi) {
+            const qg_circuit_op &op = gates[gi];
+            if (op.kind != 0) fail(QG_ERR_VALUE, "circuit %d: fixed gates only.", c);
+            if (op.target < 0 || op.target >= n || op.n_controls < 0 || op.n_controls > 4)
+                fail(QG_ERR_VALUE, "circuit %d: bad gate.", c);
+            PendingGate g;
+            g.target = op.target;
+            unsigned long long seen = 1ULL << op.target;
+            for (int k = 0; k < op.n_controls; ++k) {
+                int q = op.controls[k];
+                if (q < 0 || q >= n || (seen & (1ULL << q)))
+                    fail(QG_ERR_VALUE, "circuit %d: bad control.", c);
+                seen |= 1ULL << q;
+                g.controls.push_back(q);
+            }
+            memcpy(g.m.v, op.mat, sizeof(g.m.v));
+            g.diag = is_diag(g.m);
+            gl.push_back(g);
+        }
+        merge_runs(gl);
+        if (n <= 13) {
+            const int rl = n <= 9 ? 3 : (n <= 12 ? 4 : 5);
+            std::vector<const PendingGate *> ptrs;
+            for (auto &g : gl) ptrs.push_back(&g);
+            TileLanes tl = tile_lanes_of(n >= 64 ? ~0ULL : ((1ULL << n) - 1), n);
+            build_program<float>(ptrs, tl, rl, prog, sets);
+            if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: program too long.", c);
+            ResidentCircuit rc;
+            rc.ops_off = (long long)ops_all.size();
+            rc.nops = (int)prog.size();
+            rc.sets_off = (int)(sets_all.size() / 2);
+            rc.out_index = c;
+            rc.pad = 0;
+            ops_all.insert(ops_all.end(), prog.begin(), prog.end());
+            append_sets(sets, n, rl, sets_all);
+            res[n].push_back(rc);
+        } else {
+            const long long off = arena_elems;
+            arena_elems += ((1LL << n) + 31) & ~31LL;
+            big_off.push_back(off);
+            big_n.push_back(n);
+            big_idx.push_back(c);
+            auto plan = plan_gate_stages(gl, n, 12, 4);
+            for (size_t r = 0; r < plan.size(); ++r) {
+                TileLanes tl = tile_lanes_of(plan[r].first, n);
+                build_program<float>(plan[r].second, tl, 4, prog, sets);
+                if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: stage too long.", c);
+                BatchStage st;
+                memset(&st, 0, sizeof(st));
+                st.state_off = off;
+                st.n = n;
+                st.m = 12;
+                st.rl = 4;
+                fill_tile_header(tl, n, 4, st.lowrun, st.nhi, st.hi_pos, st.nins, st.ins_pos,
+                                 st.dep_hi);
+                st.nops = (int)prog.size();
+                st.ops_off = (long long)ops_all.size();
+                st.sets_off = (int)(sets_all.size() / 2);
+                ops_all.insert(ops_all.end(), prog.begin(), prog.end());
+                append_sets(sets, 12, 4, sets_all);
+                int sidx = (int)stages.size();
+                stages.push_back(st);
+                if (rounds.size() <= r) rounds.resize(r + 1);
+                for (long long t = 0; t < (1LL << (n - 12)); ++t)
+                    rounds[r].push_back(make_int2(sidx, (int)t));
+            }
+        }
+    }
+    std::vector<void *> owned;
+    auto up = [&](const void *src, size_t bytes) -> void * {
+        void *p = d.arena.alloc(std::max<size_t>(bytes, 16));
+        owned.push_back(p);
+        if (bytes) QG_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, d.stream));
+        return p;
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    try {
+        auto *d_ops = (RegOp<float> *)up(ops_all.data(), ops_all.size() * sizeof(RegOp<float>));
+        auto *d_sets = (unsigned *)up(sets_all.data(), sets_all.size() * sizeof(unsigned));
+        ResidentCircuit *d_res[14];
+        for (int n = 8; n <= 13; ++n)
+            d_res[n] = (ResidentCircuit *)up(res[n].data(), res[n].size() * sizeof(ResidentCircuit));
+        auto *d_stages = (BatchStage *)up(stages.data(), stages.size() * sizeof(BatchStage));
+        std::vector<int2> items_all;
+        std::vector<size_t> round_off;
+        for (auto &rd : rounds) {
+            round_off.push_back(items_all.size());
+            items_all.insert(items_all.end(), rd.begin(), rd.end());
+        }
+        auto *d_items = (int2 *)up(items_all.data(), items_all.size() * sizeof(int2));
+        auto *d_off = (long long *)up(big_off.data(), big_off.size() * sizeof(long long));
+        auto *d_n = (int *)up(big_n.data(), big_n.size() * sizeof(int));
+        auto *d_idx = (int *)up(big_idx.data(), big_idx.size() * sizeof(int));
+        const int nbig = (int)big_off.size();
+        double *d_part = (double *)d.arena.alloc(sizeof(double) * std::max<size_t>(batch_sumz_partials(nbig), 1));
+        owned.push_back(d_part);
+        double *d_out = (double *)d.arena.alloc(sizeof(double) * n_circuits);
+        owned.push_back(d_out);
+        float2 *arena = (float2 *)d.arena.alloc(std::max<long long>(arena_elems, 1) * sizeof(float2));
+        owned.push_back(arena);
+        batch_prepare();
+        QG_CUDA(cudaStreamSynchronize(d.stream));
+
+        // Record the whole batch as one CUDA graph, then launch it.
+        QG_CUDA(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            if (arena_elems)
+                QG_CUDA(cudaMemsetAsync(arena, 0, arena_elems * sizeof(float2), d.stream));
+            launch_batch_init(arena, d_off, nbig, d.stream);
+            for (int n = 8; n <= 13; ++n)
+                launch_batch_resident(n, n <= 9 ? 3 : (n <= 12 ? 4 : 5), d_res[n],
+                                      (int)res[n].size(), d_ops, d_sets, d_out, d.stream);
+            for (size_t r = 0; r < rounds.size(); ++r)
+                launch_batch_stage(d_stages, d_items + round_off[r], (int)rounds[r].size(), d_ops,
+                                   d_sets, arena, d.stream);
+            launch_batch_sumz(arena, d_off, d_n, d_idx, nbig, d_part, d_out, d.stream);
+        } catch (...) {
+            cudaStreamEndCapture(d.stream, &graph);
+            throw;
+        }
+        QG_CUDA(cudaStreamEndCapture(d.stream, &graph));
+        QG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        timed(d, "batch", [&] { QG_CUDA(cudaGraphLaunch(exec, d.stream)); });
+        QG_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * n_circuits, cudaMemcpyDeviceToHost,
+                                d.stream));
+        QG_CUDA(cudaStreamSynchronize(d.stream));
+    } catch (...) {
+        cudaStreamSynchronize(d.stream);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (void *p : owned) d.arena.release(p);
+        throw;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    for (void *p : owned) d.arena.release(p);
     QG_END
 }
 

@@ -1,0 +1,270 @@
+// Batched execution of many small circuits of uneven qubit counts (complex64).
+//
+// Circuits of up to 13 qubits never touch HBM with their state: one CTA
+// holds the whole 2^n-amplitude state in shared memory / registers, starts
+// from |0...0>, runs the circuit's register program (read from global memory,
+// L1-resident) and reduces sum_i <Z_i> in FP64.  Larger circuits live in a
+// packed arena and advance one fused stage per round: a round is one launch
+// over every (circuit, tile) work item of that round.  The host records the
+// whole sequence once as a CUDA graph.
+//
+// The reference runs circuits one at a time, one Python call chain per gate
+// (qgate/simulator/simulator.py:57-83, qgate/simulator/rop_executor.py:28-53).
+#include "qg_regstage.cuh"
+
+namespace qg {
+
+namespace {
+
+using namespace rs;
+
+typedef float R;
+typedef float2 C;
+
+// Runs ops[0..nops) on the register-resident tile.  `sets` holds 2 words per
+// register set (packed 5-bit lanes, thread-lane mask).  On return, a[] holds
+// the thread's amplitudes for register set (rbl, P0, q, e0).
+template <int RL>
+__device__ __forceinline__ void run_program(C (&a)[1 << RL], C *sm, const RegOp<R> *ops, int nops,
+                                            const unsigned *sets, unsigned tid, unsigned &e0,
+                                            unsigned &P0, unsigned (&q)[RL],
+                                            unsigned (&lanebit)[RL]) {
+    constexpr int NR = 1 << RL;
+    for (int oi = 0; oi < nops; ++oi) {
+        const RegOp<R> o = ops[oi];
+        if (o.kind == kOpTranspose) {
+            if (oi > 0) {
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+                __syncthreads();
+            }
+            const unsigned packed = sets[2 * o.reg];
+            e0 = pdep_sw(tid, sets[2 * o.reg + 1]);
+            P0 = Swz<R>::f(e0);
+#pragma unroll
+            for (int k = 0; k < RL; ++k) {
+                lanebit[k] = 1u << ((packed >> (5 * k)) & 31u);
+                q[k] = Swz<R>::f(lanebit[k]);
+            }
+#pragma unroll
+            for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
+            continue;
+        }
+        if ((e0 & o.tmask) != o.tmask) continue;
+        if (o.kind == kOpGate) {
+            MatR<R> mm;
+            mm.m00 = cmk<C>(o.m[0], o.m[1]);
+            mm.m01 = cmk<C>(o.m[2], o.m[3]);
+            mm.m10 = cmk<C>(o.m[4], o.m[5]);
+            mm.m11 = cmk<C>(o.m[6], o.m[7]);
+            QG_REG_DISPATCH(reg_gate, o.reg, a, mm, (unsigned)o.jmask);
+        } else if (o.kind == kOpSwapX) {
+            QG_REG_DISPATCH(reg_swap, o.reg, a, (unsigned)o.jmask);
+        } else if (o.kind == kOpDiagReg) {
+            C d0 = cmk<C>(o.m[0], o.m[1]), d1 = cmk<C>(o.m[6], o.m[7]);
+            QG_REG_DISPATCH(reg_diag, o.reg, a, d0, d1, (unsigned)o.jmask);
+        } else {
+            C ph = (e0 & o.tbit) ? cmk<C>(o.m[6], o.m[7]) : cmk<C>(o.m[0], o.m[1]);
+#pragma unroll
+            for (int j = 0; j < NR; ++j)
+                if ((j & o.jmask) == o.jmask) a[j] = cmul(ph, a[j]);
+        }
+    }
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double *ws) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) ws[w] = v;
+    __syncthreads();
+    double r = 0.;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) r += ws[i];
+    return r;  // thread 0
+}
+
+template <int RL>
+__global__ void __launch_bounds__(512)
+k_batch_resident(int n, const ResidentCircuit *__restrict__ circuits,
+                 const RegOp<R> *__restrict__ ops_all, const unsigned *__restrict__ sets_all,
+                 double *__restrict__ out) {
+    constexpr int NR = 1 << RL;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double ws[16];
+    C *sm = (C *)smraw;
+    const ResidentCircuit c = circuits[blockIdx.x];
+    const unsigned tid = threadIdx.x, T = blockDim.x;
+    const int size = 1 << n;
+    for (int e = tid; e < size; e += T) sm[e] = make_float2(0.f, 0.f);
+    __syncthreads();
+    if (tid == 0) sm[0] = make_float2(1.f, 0.f);  // slot of element 0 is 0
+    __syncthreads();
+    C a[NR];
+    unsigned e0 = 0, P0 = 0, q[RL], lanebit[RL];
+#pragma unroll
+    for (int k = 0; k < RL; ++k) q[k] = lanebit[k] = 0;
+    run_program<RL>(a, sm, ops_all + c.ops_off, c.nops, sets_all + 2 * c.sets_off, tid, e0, P0, q,
+                    lanebit);
+    // sum_i <Z_i> = sum_b |psi_b|^2 (n - 2 popcount(b))
+    float part = 0.f;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+        unsigned e = e0;
+#pragma unroll
+        for (int k = 0; k < RL; ++k)
+            if (j & (1 << k)) e |= lanebit[k];
+        part += (a[j].x * a[j].x + a[j].y * a[j].y) * (float)(n - 2 * __popc(e));
+    }
+    double tot = block_sum_d((double)part, ws);
+    if (tid == 0) out[c.out_index] = tot;
+}
+
+// One CTA per (stage, tile) work item of a round; tile of 2^12 amplitudes,
+// 16 per thread in registers (256 threads).
+__global__ void __launch_bounds__(256)
+k_batch_stage(const BatchStage *__restrict__ stages, const int2 *__restrict__ items,
+              const RegOp<R> *__restrict__ ops_all, const unsigned *__restrict__ sets_all,
+              C *__restrict__ arena) {
+    constexpr int RL = 4, NR = 16;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = (C *)smraw;
+    const int2 it = items[blockIdx.x];
+    const BatchStage &st = stages[it.x];
+    C *s = arena + st.state_off;
+    const int t = st.m - RL;
+    const unsigned tid = threadIdx.x;
+    const idx_t base = insert_zeros((idx_t)it.y, st.ins_pos, st.nins);
+    const int lr = st.lowrun < t ? st.lowrun : t;
+    idx_t dt = (idx_t)(tid & ((1u << lr) - 1u));
+    for (int b = lr; b < t; ++b)
+        if (tid & (1u << b)) dt |= 1LL << st.hi_pos[b - st.lowrun];
+    const unsigned pt = Swz<R>::f(tid);
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+        unsigned slot = pt ^ Swz<R>::f((unsigned)i << t);
+        cp_async_elem(&sm[slot], &s[base | dt | st.dep_hi[i]]);
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    C a[NR];
+    unsigned e0 = 0, P0 = 0, q[RL], lanebit[RL];
+#pragma unroll
+    for (int k = 0; k < RL; ++k) q[k] = lanebit[k] = 0;
+    run_program<RL>(a, sm, ops_all + st.ops_off, st.nops, sets_all + 2 * st.sets_off, tid, e0, P0,
+                    q, lanebit);
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+        unsigned slot = pt ^ Swz<R>::f((unsigned)i << t);
+        s[base | dt | st.dep_hi[i]] = sm[slot];
+    }
+}
+
+constexpr int kSumzChunks = 16;
+
+__global__ void __launch_bounds__(256)
+k_batch_sumz(const C *__restrict__ arena, const long long *__restrict__ off,
+             const int *__restrict__ nq, double *__restrict__ partials) {
+    __shared__ double ws[8];
+    const int c = blockIdx.y, n = nq[c];
+    const C *s = arena + off[c];
+    const idx_t N = (idx_t)1 << n;
+    const idx_t chunk = N / kSumzChunks;
+    const idx_t b0 = (idx_t)blockIdx.x * chunk;
+    double acc = 0.;
+    for (idx_t b = b0 + threadIdx.x; b < b0 + chunk; b += 4 * blockDim.x) {
+        float part = 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            idx_t bb = b + (idx_t)u * blockDim.x;
+            if (bb < b0 + chunk) {
+                C v = s[bb];
+                part += (v.x * v.x + v.y * v.y) * (float)(n - 2 * __popcll((unsigned long long)bb));
+            }
+        }
+        acc += (double)part;
+    }
+    double tot = block_sum_d(acc, ws);
+    if (threadIdx.x == 0) partials[(idx_t)c * kSumzChunks + blockIdx.x] = tot;
+}
+
+__global__ void k_batch_sumz_final(const double *__restrict__ partials, const int *__restrict__ idx,
+                                   int count, double *__restrict__ out) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= count) return;
+    double v = 0.;
+    for (int k = 0; k < kSumzChunks; ++k) v += partials[(idx_t)c * kSumzChunks + k];
+    out[idx[c]] = v;
+}
+
+__global__ void k_batch_init(C *arena, const long long *__restrict__ off, int count) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < count) arena[off[c]] = make_float2(1.f, 0.f);
+}
+
+}  // namespace
+
+void launch_batch_resident(int n, int rl, const ResidentCircuit *d_circuits, int count,
+                           const RegOp<float> *d_ops, const unsigned *d_sets, double *d_out,
+                           cudaStream_t stream) {
+    if (count <= 0) return;
+    size_t smem = sizeof(C) << n;
+    int threads = 1 << (n - rl);
+    auto launch = [&](auto kern) {
+        kern<<<count, threads, smem, stream>>>(n, d_circuits, d_ops, d_sets, d_out);
+    };
+    switch (rl) {
+    case 3: launch(k_batch_resident<3>); break;
+    case 4: launch(k_batch_resident<4>); break;
+    case 5: launch(k_batch_resident<5>); break;
+    default: fail(2, "batch: unsupported register lanes %d", rl);
+    }
+    QG_CUDA(cudaGetLastError());
+}
+
+void launch_batch_stage(const BatchStage *d_stages, const int2 *d_items, int n_items,
+                        const RegOp<float> *d_ops, const unsigned *d_sets, float2 *arena,
+                        cudaStream_t stream) {
+    if (n_items <= 0) return;
+    size_t smem = sizeof(C) << 12;
+    k_batch_stage<<<n_items, 256, smem, stream>>>(d_stages, d_items, d_ops, d_sets, arena);
+    QG_CUDA(cudaGetLastError());
+}
+
+size_t batch_sumz_partials(int count) { return (size_t)kSumzChunks * count; }
+
+void launch_batch_sumz(const float2 *arena, const long long *d_off, const int *d_n,
+                       const int *d_out_index, int count, double *d_partials, double *d_out,
+                       cudaStream_t stream) {
+    if (count <= 0) return;
+    dim3 grid(kSumzChunks, count);
+    k_batch_sumz<<<grid, 256, 0, stream>>>(arena, d_off, d_n, d_partials);
+    k_batch_sumz_final<<<(count + 127) / 128, 128, 0, stream>>>(d_partials, d_out_index, count,
+                                                                d_out);
+    QG_CUDA(cudaGetLastError());
+}
+
+// Shared-memory opt-in for every batch kernel; called before a graph capture
+// (no attribute changes while capturing).
+void batch_prepare() {
+    QG_CUDA(cudaFuncSetAttribute(k_batch_resident<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(C) << 13)));
+    QG_CUDA(cudaFuncSetAttribute(k_batch_resident<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(C) << 13)));
+    QG_CUDA(cudaFuncSetAttribute(k_batch_resident<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(C) << 13)));
+    QG_CUDA(cudaFuncSetAttribute(k_batch_stage, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(C) << 12)));
+}
+
+void launch_batch_init(float2 *arena, const long long *d_off, int count, cudaStream_t stream) {
+    if (count <= 0) return;
+    k_batch_init<<<(count + 127) / 128, 128, 0, stream>>>(arena, d_off, count);
+    QG_CUDA(cudaGetLastError());
+}
+
+}  // namespace qg

@@ -184,6 +184,45 @@ void launch_pauli_sum_apply(int prec, const void *psi, void *lam, int n, int bat
 int pauli_sum_blocks();
 void launch_sum_rows(const double *partials, int rows, int cols, double *out, cudaStream_t stream);
 
+// ---------------------------------------------------------------- batches
+
+// Tile mapping of one stage of one circuit of a batch (the RStageDesc header
+// without the program), in device memory.
+struct BatchStage {
+    long long state_off;  // element offset of the circuit's state in the arena
+    int n, m, rl, lowrun, nhi, nins, nops;
+    int hi_pos[kMaxTileLanes];
+    int ins_pos[kMaxTileLanes];
+    long long dep_hi[1 << kMaxRegLanes];
+    long long ops_off;    // index of the stage's first RegOp in the program buffer
+    int sets_off;         // index of the stage's first register set
+    int pad;
+};
+
+// Circuits that fit one CTA: 2^n amplitudes of complex64 in shared memory,
+// whole gate program, then sum_i <Z_i> (FP64) to out[circuit].
+struct ResidentCircuit {
+    long long ops_off;
+    int nops, sets_off, out_index, pad;
+};
+
+void launch_batch_resident(int n, int rl, const ResidentCircuit *d_circuits, int count,
+                           const RegOp<float> *d_ops, const unsigned *d_sets, double *d_out,
+                           cudaStream_t stream);
+// One round: every (stage, tile) work item of the round.  d_items[i] =
+// {stage index, tile index}.
+void launch_batch_stage(const BatchStage *d_stages, const int2 *d_items, int n_items,
+                        const RegOp<float> *d_ops, const unsigned *d_sets, float2 *arena,
+                        cudaStream_t stream);
+// out[out_index[c]] = sum_i <Z_i> over 2^n_c amplitudes at arena + off[c];
+// FP64; d_partials holds batch_sumz_partials(count) doubles.
+size_t batch_sumz_partials(int count);
+void launch_batch_sumz(const float2 *arena, const long long *d_off, const int *d_n,
+                       const int *d_out_index, int count, double *d_partials, double *d_out,
+                       cudaStream_t stream);
+void launch_batch_init(float2 *arena, const long long *d_off, int count, cudaStream_t stream);
+void batch_prepare();
+
 // Engine services for other translation units.
 cudaStream_t engine_stream();
 void *engine_alloc(size_t bytes);

@@ -1,0 +1,45 @@
+"""GPU parity of batched uneven circuits (sum_i <Z_i> per circuit) against
+the oracle's complex128 runs."""
+import numpy as np
+import pytest
+
+from oracle import statevec as sv
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_sum_z(n, ops):
+    psi = sv.run_ops(n, [('g', nm, a, False, t, c) for nm, a, t, c in ops], np.complex128)
+    return sum(2 * sv.calc_probability(psi, q) - 1 for q in range(n))
+
+
+def test_batch_sizes_8_to_20():
+    from qgate_gb300.batch import hea_batch, sum_z
+    circuits = hea_batch(count=60, seed=3, min_qubits=8, max_qubits=20, min_depth=2, max_depth=6)
+    got = sum_z(circuits)
+    for (n, ops), g in zip(circuits, got):
+        want = _oracle_sum_z(n, ops)
+        assert abs(g - want) < 2e-5 * n, (n, g, want)
+
+
+def test_batch_mixed_gates_and_controls():
+    """Dense random gates with controls, every size from 8 to 16."""
+    from qgate_gb300.batch import sum_z
+    from tests.gpu_helpers import random_ops
+    rng = np.random.default_rng(8)
+    circuits = []
+    for n in range(8, 17):
+        ops = [(nm, a, t, c) for _, nm, a, adj, t, c in random_ops(rng, n, 80, max_controls=3)
+               if not adj]
+        circuits.append((n, ops))
+    got = sum_z(circuits)
+    for (n, ops), g in zip(circuits, got):
+        assert abs(g - _oracle_sum_z(n, ops)) < 2e-5 * n
+
+
+def test_batch_repeatable_and_order_independent():
+    from qgate_gb300.batch import hea_batch, sum_z
+    circuits = hea_batch(count=40, seed=4, max_qubits=16)
+    a = sum_z(circuits)
+    b = sum_z(circuits[::-1])[::-1]
+    assert np.array_equal(a, b)
