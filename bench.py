@@ -220,12 +220,8 @@ def config_block(args, extra):
 
 def run_gb300(args):
     import torch
-    world = int(os.environ.get('WORLD_SIZE', '1'))
-    rank = int(os.environ.get('RANK', '0'))
-    local = int(os.environ.get('LOCAL_RANK', '0'))
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group('gloo')
+    from qgate_gb300 import replicas
+    world, rank, local = replicas.init()
     torch.cuda.set_device(local)
 
     from qgate_gb300 import _native as nat
@@ -265,8 +261,7 @@ def run_gb300(args):
     nat.timing_all(reset=True)
     sampler = ClockSampler(local)
     sampler.start()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     nat.timing_enable(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -282,12 +277,9 @@ def run_gb300(args):
     timing = nat.timing_all(reset=True)
     init_bytes = (1 << n) * cs * args.steps
     moved = stats['bytes'] + init_bytes
-    t_max = dev_ms
-    if world > 1:
-        t = torch.tensor([dev_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t[0])
-    value = unfused_bytes * args.steps * world / (t_max / 1e3) / 1e9
+    value, t_max_s = replicas.aggregate_throughput(unfused_bytes * args.steps, dev_ms / 1e3)
+    value /= 1e9
+    t_max = t_max_s * 1e3
     hbm_actual = moved * world / (t_max / 1e3) / 1e9
     launches = sum(v[0] for v in timing.values())
 
@@ -302,7 +294,7 @@ def run_gb300(args):
         alg = stats['bytes'] / max(1, stats['passes'])
         traffic = None
     achieved = alg / (dom_ms / dom_launches / 1e3) / 1e9 if dom_launches else 0.
-    roofline = {'kernel': {'stage': 'k_stage (fused shared-memory stage)',
+    roofline = {'kernel': {'stage': 'k_rstage (fused register-resident stage)',
                            'gate': 'k_pairs (single gate)'}.get(dom_name, dom_name),
                 'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                 'frac': achieved / peak, 'peak_source': peak_kind,
@@ -321,10 +313,17 @@ def run_gb300(args):
     if rank == 0 and not args.no_batch:
         batch = run_batch(args, nat)
 
+
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         qs.delete()
         adjoint = run_adjoint(args)
+
+    c4 = None
+    if rank == 0 and args.c4:
+        qs.delete()
+        nat.call('qg_devices_clear')
+        c4 = run_c4(args, rt, nat)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -355,6 +354,7 @@ def run_gb300(args):
             'roofline': roofline,
             'adjoint': adjoint,
             'batch': batch,
+            'large_states': c4,
             'cpu_baseline': cpu,
             'e2e': e2e,
             'gpu_launches': launches,
@@ -362,9 +362,7 @@ def run_gb300(args):
             'clocks': clocks,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.barrier()
-        torch.distributed.destroy_process_group()
+    replicas.finish()
 
 
 def single_gate_passes(nat, proc, qs, gts, n, cs, torch, count=8):
@@ -431,6 +429,89 @@ def run_adjoint(args):
     out['max_grad_err_fp32_vs_fp64'] = float(np.max(np.abs(res['fp32'][1] - res['fp64'][1])))
     out['max_energy_err_fp32_vs_fp64'] = float(np.max(np.abs(res['fp32'][0] - res['fp64'][0])))
     out['checkpoint_every_gates_fp32'] = 3 * 3 * n
+    return out
+
+
+def qft_ops(n, seed):
+    """QFT without final swaps on |x>, X on qubit i iff rng.random() < 0.5
+    (in qubit order): for i: H(q_i), then CU1(pi / 2^(j-i)) controlled by q_j
+    on q_i for j > i."""
+    rng = np.random.default_rng(seed)
+    ops = [('X', (), q, ()) for q in range(n) if rng.random() < 0.5]
+    for i in range(n):
+        ops.append(('H', (), i, ()))
+        for j in range(i + 1, n):
+            ops.append(('U1', (math.pi / (1 << (j - i)),), i, (j,)))
+    return ops
+
+
+def run_c4(args, rt, nat):
+    """Large single states: a 33-qubit depth-30 random U3+CX circuit
+    (default_rng(40)), and a 34-qubit QFT (X preparation from default_rng(41))
+    followed by an FP64 sampling pool and 1e8 samples (default_rng(42)), all
+    complex64.  The QFT of a basis state has every probability equal to 2^-34,
+    so Pr(q = 0) = 1/2 for every qubit and the uniform (k + 1/2) / 2^34 samples
+    index k."""
+    from qgate_gb300.circuit import gate_type, Lane
+    from qgate_gb300 import autotune
+    out = {}
+
+    def run(n, ops, label):
+        gts = [(gate_type(nm, *a), t, list(c)) for nm, a, t, c in ops]
+        qs = rt.create_qubit_states(np.float32)
+        proc = qs.processor
+        proc.initialize_qubit_states(qs, n)
+        proc.reset_qubit_states(qs)
+        proc.synchronize()
+        nat.gate_stats(reset=True)
+        t0 = time.perf_counter()
+        for gt, t, c in gts:
+            if c:
+                proc.apply_controlled_gate(gt, False, qs, c, t)
+            else:
+                proc.apply_gate(gt, False, qs, t)
+        proc.synchronize()
+        dt = time.perf_counter() - t0
+        st = nat.gate_stats(reset=True)
+        out[label] = {'qubits': n, 'gates': len(ops), 'passes': st['passes'], 'ms': dt * 1e3,
+                      'gate_pass_gbs': gate_pass_bytes(n, ops, 8) / dt / 1e9,
+                      'hbm_gbs_actual': st['bytes'] / dt / 1e9,
+                      'norm': qs.processor.calc_norm(qs)}
+        return qs
+
+    n1 = args.c4_random_qubits
+    ops1 = circuit(n1, 30, seed_angles=40, seed_perm=40)
+    cached = autotune._load().get(autotune._key(30, np.float32))
+    if cached:
+        autotune.apply(cached)
+    qs = run(n1, ops1, 'random_%dq_depth30' % n1)
+    qs.delete()
+    nat.call('qg_devices_clear')  # return the cached 64 GiB before the 128 GiB state
+
+    n2 = args.c4_qft_qubits
+    qs = run(n2, qft_ops(n2, 41), 'qft_%dq' % n2)
+    pr = [qs.processor.calc_probability(qs, q) for q in range(0, n2, 5)]
+    out['qft_%dq' % n2]['max_abs_pr0_minus_half'] = float(max(abs(p - 0.5) for p in pr))
+    getter = rt.create_qubits_states_getter(np.float32)
+    t0 = time.perf_counter()
+    pool = getter.create_sampling_pool(list(range(n2)), n2, 0,
+                                       [(qs, [Lane(l, l) for l in range(n2)])], [])
+    t_pool = time.perf_counter() - t0
+    u = np.random.default_rng(42).random(args.c4_samples)
+    t0 = time.perf_counter()
+    obs = pool.sample(len(u), u)
+    t_samp = time.perf_counter() - t0
+    N = 1 << n2
+    k = np.random.default_rng(43).integers(0, N, 100000)
+    mid = pool.sample(len(k), (k + 0.5) / N)
+    dev = np.abs(np.asarray(mid.intarray) - k)
+    out['pool'] = {'entries': N, 'create_ms': t_pool * 1e3, 'samples': len(u),
+                   'sample_ms': t_samp * 1e3, 'samples_per_s': len(u) / t_samp,
+                   'midpoint_exact_frac': float(np.mean(dev == 0)),
+                   'midpoint_max_index_dev': int(dev.max())}
+    pool.delete()
+    qs.delete()
+    nat.call('qg_devices_clear')
     return out
 
 
@@ -513,6 +594,10 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
+    ap.add_argument('--c4', action='store_true', help='also run the 33/34-qubit large states')
+    ap.add_argument('--c4-random-qubits', type=int, default=33)
+    ap.add_argument('--c4-qft-qubits', type=int, default=34)
+    ap.add_argument('--c4-samples', type=int, default=100_000_000)
     ap.add_argument('--batch-circuits', type=int, default=4096)
     ap.add_argument('--batch-steps', type=int, default=3)
     ap.add_argument('--adj-qubits', type=int, default=24)

@@ -145,6 +145,10 @@ int qg_set_fusion(int max_tile_lanes);
  * by the register-resident stage kernel (3..5; complex128 at most 4), and a
  * per-amplitude instruction budget that closes a stage early (0 = none). */
 int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budget);
+/* Extension: 1 runs large fused stages with the persistent, double-buffered
+ * stage kernel; 0 (default) with one CTA per tile, which keeps more warps
+ * resident per SM. */
+int qg_set_stage_pipelining(int on);
 /* Extension: counters of the gate path since the last reset
  * {gates, passes, bytes_moved}. */
 int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset);

@@ -54,6 +54,7 @@ SIGNATURES = {
     'qg_qubit_processor_calc_norm': [_h, _h, _dp],
     'qg_set_fusion': [_i],
     'qg_set_fusion_params': [_i, _i, _i, _i],
+    'qg_set_stage_pipelining': [_i],
     'qg_gate_stats': [_i64p, _i64p, _i64p, _i],
     'qg_timing_enable': [_i],
     'qg_timing_read': [ctypes.c_char_p, _i64p, _dp, _i],

@@ -153,6 +153,7 @@ struct Device {
     int tile_lanes[3] = {0, 12, 13};
     int reg_lanes[3] = {0, 4, 4};
     int cost_budget[3] = {0, 0, 0};
+    bool pipelined = false;  // persistent double-buffered stage kernel (opt-in)
     long long n_gates = 0, n_passes = 0, n_bytes = 0;
     // Per-kernel-class launch timing with CUDA events on the engine's stream.
     bool timing = false;
@@ -508,11 +509,11 @@ static void run_stage(Device &d, States *s, unsigned long long S,
     if (s->prec == kFP32) {
         static RStageDesc<float> desc;
         ok = schedule_rstage(gates, tl, n, rl, desc);
-        if (ok) timed(d, "stage", [&] { launch_rstage_f32(s->d, desc, d.stream); });
+        if (ok) timed(d, "stage", [&] { launch_rstage_f32(s->d, desc, d.stream, d.pipelined); });
     } else {
         static RStageDesc<double> desc;
         ok = schedule_rstage(gates, tl, n, rl, desc);
-        if (ok) timed(d, "stage", [&] { launch_rstage_f64(s->d, desc, d.stream); });
+        if (ok) timed(d, "stage", [&] { launch_rstage_f64(s->d, desc, d.stream, d.pipelined); });
     }
     if (!ok) {
         // Program too long for one descriptor: split the stage.
@@ -655,6 +656,24 @@ static double read_result(Device &d, double *d_val) {
 
 // ------------------------------------------------------------ transfers
 
+// Host-side copy between pinned staging and the caller's (pageable) buffer,
+// split over OpenMP threads: one host thread copies ~10-20 GB/s, well below
+// what NVLink-C2C delivers into the staging buffers.
+static void host_copy(void *dst, const void *src, size_t bytes) {
+    const size_t kSlice = 4u << 20;
+    if (bytes < 2 * kSlice) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    const long long nslices = (long long)((bytes + kSlice - 1) / kSlice);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < nslices; ++i) {
+        size_t off = (size_t)i * kSlice;
+        size_t len = std::min(kSlice, bytes - off);
+        memcpy((char *)dst + off, (const char *)src + off, len);
+    }
+}
+
 // Device buffer -> host, through two pinned staging buffers so that the
 // host-side copy of one chunk overlaps the transfer of the next.
 // `produce(chunk_begin, chunk_count, dbuf)` fills dbuf on the stream.
@@ -671,7 +690,7 @@ static void staged_d2h(Device &d, void *host, idx_t count, size_t item, F produc
             int b = (int)(c & 1);
             if (c >= 2 && pend_cnt[b] > 0) {
                 QG_CUDA(cudaEventSynchronize(d.ev[b]));
-                memcpy((char *)host + pend_begin[b] * item, d.h_stage[b], pend_cnt[b] * item);
+                host_copy((char *)host + pend_begin[b] * item, d.h_stage[b], pend_cnt[b] * item);
                 pend_cnt[b] = 0;
             }
             if (c < nchunks) {
@@ -1212,6 +1231,13 @@ int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budge
     QG_END
 }
 
+int qg_set_stage_pipelining(int on) {
+    QG_BEGIN
+    flush_all();
+    g_dev.pipelined = on != 0;
+    QG_END
+}
+
 int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset) {
     QG_BEGIN
     *gates = g_dev.n_gates;
@@ -1668,7 +1694,7 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
     try {
         for (idx_t b = 0; b < n_samples; b += chunk) {
             idx_t cnt = std::min(chunk, (idx_t)n_samples - b);
-            memcpy(d.h_stage[0], randnum + b, cnt * 8);
+            host_copy(d.h_stage[0], randnum + b, cnt * 8);
             QG_CUDA(cudaMemcpyAsync(du, d.h_stage[0], cnt * 8, cudaMemcpyHostToDevice, d.stream));
             timed(d, "search", [&] {
                 launch_search(p->cdf, p->n, du, dobs, cnt, p->empty_pos.data(),
@@ -1676,7 +1702,7 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
             });
             QG_CUDA(cudaMemcpyAsync(d.h_stage[1], dobs, cnt * 8, cudaMemcpyDeviceToHost, d.stream));
             QG_CUDA(cudaStreamSynchronize(d.stream));
-            memcpy(obs + b, d.h_stage[1], cnt * 8);
+            host_copy(obs + b, d.h_stage[1], cnt * 8);
         }
     } catch (...) {
         d.arena.release(du);

@@ -81,13 +81,14 @@ def build(force=False, verbose=False, ptxas_verbose=False):
         objs.append(o)
         if force or _stale(o, s):
             cxx = os.environ.get('CXX', 'g++')
-            jobs.append([cxx, '-O2', '-std=c++17', '-fPIC', '-Wall', '-c', s, '-o', o] + inc)
+            jobs.append([cxx, '-O2', '-std=c++17', '-fPIC', '-Wall', '-fopenmp', '-c', s, '-o', o] + inc)
     outputs = []
     if jobs:
         with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             outputs = list(ex.map(lambda c: _run(c, verbose), jobs))
     if jobs or not os.path.exists(LIB):
-        _run([nvcc] + ARCH + ['-shared', '-cudart', 'static', '-o', LIB] + objs, verbose)
+        _run([nvcc] + ARCH + ['-shared', '-cudart', 'static', '-Xcompiler', '-fopenmp', '-o', LIB] +
+             objs + ['-lgomp'], verbose)
     return LIB, outputs
 
 

@@ -103,21 +103,21 @@ k_stage(typename CT<R>::type *__restrict__ s, const __grid_constant__ StageDesc 
 // reads it with broadcast vector loads instead of per-field constant-bank
 // loads.  Load (cp.async, coalesced, swizzled) -> run the program (register
 // gates, diagonal phases, shared-memory transposes) -> store.
-template <class R, int RL>
-__global__ void __launch_bounds__(RL >= 5 ? 256 : 512)
+template <class R, int RL, int TL>
+__global__ void __launch_bounds__(1 << TL)
 k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDesc<R> d) {
     typedef typename CT<R>::type C;
     typedef RegOp<R> Op;
     constexpr int NR = 1 << RL;
+    constexpr int t = TL;                 // thread lanes (tile lanes 0..t-1)
+    constexpr int m = RL + TL;            // tile lanes
+    constexpr unsigned T = 1u << TL;
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int m = d.m;
     C *sm = (C *)smraw;
     Op *sops = (Op *)(smraw + ((size_t)sizeof(C) << m));
     long long *sdep = (long long *)(sops + d.nops);
     unsigned *sset = (unsigned *)(sdep + NR);  // per set: rb lanes packed 5x5 bits, tbmask
-    const int t = m - RL;
     const unsigned tid = threadIdx.x;
-    const unsigned T = blockDim.x;
 
     {
         const int4 *src = (const int4 *)d.ops;
@@ -133,19 +133,20 @@ k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDes
         }
     }
     const idx_t base = insert_zeros((idx_t)blockIdx.x, d.ins_pos, d.nins);
-    // Global offset of tile element tid (tile lanes 0..t-1).
+    // Global offset of tile element tid (tile lanes 0..t-1); the offsets of
+    // the register-index parts (i << t) are disjoint from it, so element
+    // (tid, i) lives at gp + dep_hi[i].
     const int lr = d.lowrun < t ? d.lowrun : t;
     idx_t dt = (idx_t)(tid & ((1u << lr) - 1u));
     for (int b = lr; b < t; ++b)
         if (tid & (1u << b)) dt |= 1LL << d.hi_pos[b - d.lowrun];
+    C *const gp = s + (base | dt);
     const unsigned pt = Swz<R>::f(tid);
     __syncthreads();
 
 #pragma unroll
-    for (int i = 0; i < NR; ++i) {
-        unsigned slot = pt ^ Swz<R>::f((unsigned)i << t);
-        cp_async_elem(&sm[slot], &s[base | dt | sdep[i]]);
-    }
+    for (int i = 0; i < NR; ++i)
+        cp_async_elem(&sm[pt ^ Swz<R>::f((unsigned)i << t)], gp + sdep[i]);
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
 
@@ -200,32 +201,176 @@ k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDes
     for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < NR; ++i) {
-        unsigned slot = pt ^ Swz<R>::f((unsigned)i << t);
-        s[base | dt | sdep[i]] = sm[slot];
+    for (int i = 0; i < NR; ++i) gp[sdep[i]] = sm[pt ^ Swz<R>::f((unsigned)i << t)];
+}
+
+// Persistent, double-buffered variant: a grid of (SMs x resident CTAs)
+// walks the tiles; each CTA copies the stage program to shared memory once,
+// then prefetches tile k+1 (cp.async into the other buffer) while it runs the
+// program on tile k and writes tile k back, so HBM stays busy during the
+// arithmetic.
+template <class R, int RL, int TL>
+__global__ void __launch_bounds__(1 << TL)
+k_rstage_pipe(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDesc<R> d,
+              long long tiles) {
+    typedef typename CT<R>::type C;
+    typedef RegOp<R> Op;
+    constexpr int NR = 1 << RL;
+    constexpr int t = TL;
+    constexpr int m = RL + TL;
+    constexpr unsigned T = 1u << TL;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *buf0 = (C *)smraw;
+    C *buf1 = buf0 + (1 << m);
+    Op *sops = (Op *)(smraw + ((size_t)sizeof(C) << (m + 1)));
+    long long *sdep = (long long *)(sops + d.nops);
+    unsigned *sset = (unsigned *)(sdep + NR);
+    const unsigned tid = threadIdx.x;
+    {
+        const int4 *src = (const int4 *)d.ops;
+        int4 *dst = (int4 *)sops;
+        const int nvec = (int)(d.nops * sizeof(Op) / sizeof(int4));
+        for (int i = tid; i < nvec; i += T) dst[i] = src[i];
+        if (tid < (unsigned)NR) sdep[tid] = d.dep_hi[tid];
+        for (int i = tid; i < kMaxRegSets; i += T) {
+            unsigned packed = 0;
+            for (int k = 0; k < RL; ++k) packed |= (unsigned)d.rb[i][k] << (5 * k);
+            sset[2 * i] = packed;
+            sset[2 * i + 1] = d.tbmask[i];
+        }
+    }
+    const int lr = d.lowrun < t ? d.lowrun : t;
+    idx_t dt = (idx_t)(tid & ((1u << lr) - 1u));
+    for (int b = lr; b < t; ++b)
+        if (tid & (1u << b)) dt |= 1LL << d.hi_pos[b - d.lowrun];
+    const unsigned pt = Swz<R>::f(tid);
+    __syncthreads();
+
+    const long long G = gridDim.x;
+    long long tile = blockIdx.x;
+    if (tile >= tiles) return;
+    auto issue = [&](long long tl, C *buf) {
+        C *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
+#pragma unroll
+        for (int i = 0; i < NR; ++i)
+            cp_async_elem(&buf[pt ^ Swz<R>::f((unsigned)i << t)], gp + sdep[i]);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    issue(tile, buf0);
+    const int nops = d.nops;
+    for (int k = 0; tile < tiles; ++k, tile += G) {
+        C *sm = (k & 1) ? buf1 : buf0;
+        const long long next = tile + G;
+        if (next < tiles) {
+            issue(next, (k & 1) ? buf0 : buf1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        __syncthreads();
+
+        C a[NR];
+        unsigned e0 = 0, P0 = 0;
+        unsigned q[RL];
+#pragma unroll
+        for (int kk = 0; kk < RL; ++kk) q[kk] = 0;
+        for (int oi = 0; oi < nops; ++oi) {
+            const Op o = sops[oi];
+            if (o.kind == kOpTranspose) {
+                if (oi > 0) {
+                    __syncthreads();
+#pragma unroll
+                    for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+                    __syncthreads();
+                }
+                const unsigned packed = sset[2 * o.reg];
+                e0 = pdep_sw(tid, sset[2 * o.reg + 1]);
+                P0 = Swz<R>::f(e0);
+#pragma unroll
+                for (int kk = 0; kk < RL; ++kk)
+                    q[kk] = Swz<R>::f(1u << ((packed >> (5 * kk)) & 31u));
+#pragma unroll
+                for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
+                continue;
+            }
+            if ((e0 & o.tmask) != o.tmask) continue;
+            if (o.kind == kOpGate) {
+                MatR<R> mm;
+                mm.m00 = cmk<C>(o.m[0], o.m[1]);
+                mm.m01 = cmk<C>(o.m[2], o.m[3]);
+                mm.m10 = cmk<C>(o.m[4], o.m[5]);
+                mm.m11 = cmk<C>(o.m[6], o.m[7]);
+                QG_REG_DISPATCH(reg_gate, o.reg, a, mm, (unsigned)o.jmask);
+            } else if (o.kind == kOpSwapX) {
+                QG_REG_DISPATCH(reg_swap, o.reg, a, (unsigned)o.jmask);
+            } else if (o.kind == kOpDiagReg) {
+                C d0 = cmk<C>(o.m[0], o.m[1]), d1 = cmk<C>(o.m[6], o.m[7]);
+                QG_REG_DISPATCH(reg_diag, o.reg, a, d0, d1, (unsigned)o.jmask);
+            } else {
+                C ph = (e0 & o.tbit) ? cmk<C>(o.m[6], o.m[7]) : cmk<C>(o.m[0], o.m[1]);
+#pragma unroll
+                for (int j = 0; j < NR; ++j)
+                    if ((j & o.jmask) == o.jmask) a[j] = cmul(ph, a[j]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+        __syncthreads();
+        C *gp = s + (insert_zeros((idx_t)tile, d.ins_pos, d.nins) | dt);
+#pragma unroll
+        for (int i = 0; i < NR; ++i) gp[sdep[i]] = sm[pt ^ Swz<R>::f((unsigned)i << t)];
+        __syncthreads();  // the buffer is refilled two iterations later
     }
 }
 
 template <class R>
-void rstage_dispatch(void *state, const RStageDesc<R> &d, cudaStream_t stream) {
+void rstage_dispatch(void *state, const RStageDesc<R> &d, cudaStream_t stream, bool pipelined) {
     typedef typename CT<R>::type C;
-    size_t smem = ((size_t)1 << d.m) * sizeof(C) + (size_t)d.nops * sizeof(RegOp<R>) +
-                  sizeof(long long) * (1 << d.rl) + sizeof(unsigned) * 2 * kMaxRegSets;
+    const size_t prog = (size_t)d.nops * sizeof(RegOp<R>) + sizeof(long long) * (1 << d.rl) +
+                        sizeof(unsigned) * 2 * kMaxRegSets;
+    const size_t tile_bytes = ((size_t)1 << d.m) * sizeof(C);
     idx_t tiles = (idx_t)1 << (d.n - d.m);
     int threads = 1 << (d.m - d.rl);
     if (threads < 32 || threads > (d.rl >= 5 ? 256 : 512))
         fail(2, "register stage: bad tile shape m=%d rl=%d", d.m, d.rl);
+    // Pipelining needs two tiles per CTA and several tiles per CTA to pay off.
+    const size_t pipe_smem = 2 * tile_bytes + prog;
+    if (pipelined && (pipe_smem > 227 * 1024 || tiles < 2 * 152)) pipelined = false;
     auto launch = [&](auto kern) {
+        const size_t smem = tile_bytes + prog;
         QG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<(unsigned)tiles, threads, smem, stream>>>((C *)state, d);
     };
-    switch (d.rl) {
-    case 3: launch(k_rstage<R, 3>); break;
-    case 4: launch(k_rstage<R, 4>); break;
-    case 5: launch(k_rstage<R, 5>); break;
-    default: fail(2, "register stage: unsupported register lanes %d", d.rl);
+    auto launch_pipe = [&](auto kern) {
+        QG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)pipe_smem));
+        int per_sm = 0, sms = 0, dev = 0;
+        QG_CUDA(cudaGetDevice(&dev));
+        QG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        QG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, pipe_smem));
+        if (per_sm < 1) per_sm = 1;
+        long long grid = (long long)sms * per_sm;
+        if (grid > tiles) grid = tiles;
+        kern<<<(unsigned)grid, threads, pipe_smem, stream>>>((C *)state, d, (long long)tiles);
+    };
+    const int tl = d.m - d.rl;
+#define QG_RS_CASE(RL_, TL_)                                        \
+    if (d.rl == RL_ && tl == TL_) {                                 \
+        if (pipelined)                                              \
+            launch_pipe(k_rstage_pipe<R, RL_, TL_>);                \
+        else                                                        \
+            launch(k_rstage<R, RL_, TL_>);                          \
+        QG_CUDA(cudaGetLastError());                                \
+        return;                                                     \
     }
-    QG_CUDA(cudaGetLastError());
+    QG_RS_CASE(3, 5) QG_RS_CASE(3, 6) QG_RS_CASE(3, 7) QG_RS_CASE(3, 8) QG_RS_CASE(3, 9)
+    QG_RS_CASE(4, 5) QG_RS_CASE(4, 6) QG_RS_CASE(4, 7) QG_RS_CASE(4, 8) QG_RS_CASE(4, 9)
+    if constexpr (sizeof(R) == 4) {
+        QG_RS_CASE(5, 5) QG_RS_CASE(5, 6) QG_RS_CASE(5, 7) QG_RS_CASE(5, 8)
+    }
+#undef QG_RS_CASE
+    fail(2, "register stage: unsupported shape m=%d rl=%d", d.m, d.rl);
 }
 
 }  // namespace
@@ -247,12 +392,14 @@ void launch_stage(int prec, void *state, const StageDesc &d, cudaStream_t stream
     QG_CUDA(cudaGetLastError());
 }
 
-void launch_rstage_f32(void *state, const RStageDesc<float> &d, cudaStream_t stream) {
-    rstage_dispatch<float>(state, d, stream);
+void launch_rstage_f32(void *state, const RStageDesc<float> &d, cudaStream_t stream,
+                       bool pipelined) {
+    rstage_dispatch<float>(state, d, stream, pipelined);
 }
 
-void launch_rstage_f64(void *state, const RStageDesc<double> &d, cudaStream_t stream) {
-    rstage_dispatch<double>(state, d, stream);
+void launch_rstage_f64(void *state, const RStageDesc<double> &d, cudaStream_t stream,
+                       bool pipelined) {
+    rstage_dispatch<double>(state, d, stream, pipelined);
 }
 
 }  // namespace qg

@@ -124,8 +124,12 @@ template <class R> struct RStageDesc {
     RegOp<R> ops[kMaxRegOps];                     // 16-byte aligned
 };
 
-void launch_rstage_f32(void *state, const RStageDesc<float> &d, cudaStream_t stream);
-void launch_rstage_f64(void *state, const RStageDesc<double> &d, cudaStream_t stream);
+// pipelined: persistent grid with double-buffered tiles (when the state has
+// enough tiles and two fit in shared memory).
+void launch_rstage_f32(void *state, const RStageDesc<float> &d, cudaStream_t stream,
+                       bool pipelined);
+void launch_rstage_f64(void *state, const RStageDesc<double> &d, cudaStream_t stream,
+                       bool pipelined);
 
 // ---------------------------------------------------------------- adjoint
 

@@ -131,6 +131,36 @@ def test_register_stage_shapes(rt, dtype):
 
 
 @pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_pipelined_stage_kernel_22q(rt, dtype):
+    """The persistent double-buffered stage kernel (used once a state has
+    >= 304 tiles): 22 qubits, several tile shapes, against the oracle and
+    against the one-CTA-per-tile kernel (bit-identical: same arithmetic)."""
+    from qgate_gb300 import _native as nat
+    prec = nat.PREC_FP64 if dtype == np.float64 else nat.PREC_FP32
+    rng = np.random.default_rng(22)
+    n = 22
+    ops = random_ops(rng, n, 90, max_controls=2)
+    want = sv.run_ops(n, ops, np.complex128)
+    tol = 1e-11 if dtype == np.float64 else 1e-5
+    shapes = [(11, 4), (12, 4), (13, 4)] + ([(12, 5), (13, 5)] if dtype == np.float32 else [])
+    try:
+        for tile, rl in shapes:
+            nat.set_fusion_params(prec, tile, rl, 0)
+            got = {}
+            for pipe in (1, 0):
+                nat.call('qg_set_stage_pipelining', pipe)
+                qs = new_state(rt, n, dtype)
+                apply_ops(qs, ops)
+                got[pipe] = qs.get_raw()
+                qs.delete()
+            assert np.max(np.abs(got[1] - want)) < tol, (tile, rl)
+            assert np.array_equal(got[1], got[0]), (tile, rl)
+    finally:
+        nat.call('qg_set_stage_pipelining', 0)
+        nat.set_fusion(0)
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
 def test_random_circuit_20q_fidelity(rt, dtype):
     """20 qubits, U3 layers + CX matchings (the 30-qubit benchmark circuit's
     structure at a size the oracle finishes in seconds)."""
