@@ -47,6 +47,11 @@ __device__ __forceinline__ void reg_grad(const C (&a)[NR], const C (&l)[NR], uns
     out = acc;
 }
 
+// Shared-memory bytes of n register-set slot tables, rounded to 16.
+__host__ __device__ constexpr unsigned adj_sets_bytes(int nsets) {
+    return ((unsigned)nsets * (unsigned)sizeof(SetSlots) + 15u) & ~15u;
+}
+
 template <class R> __device__ __forceinline__ R warp_sum(R v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -71,8 +76,8 @@ k_adj_stage(typename CT<R>::type *__restrict__ psi_all, typename CT<R>::type *__
     C *sl = sp + (MODE == 1 ? (1 << m) : 0);
     AdjOp *sops = (AdjOp *)(sp + ((MODE == 1 ? 2 : 1) << m));
     long long *sdep = (long long *)(sops + d.nops);
-    unsigned *sset = (unsigned *)(sdep + NR);
-    R *smat = (R *)(sset + 2 * kMaxRegSets);
+    SetSlots *sset = (SetSlots *)(sdep + NR);
+    R *smat = (R *)((unsigned char *)sset + adj_sets_bytes(d.nsets));
     R *sgrad = smat + 8 * d.nmats;
 
     {
@@ -80,12 +85,7 @@ k_adj_stage(typename CT<R>::type *__restrict__ psi_all, typename CT<R>::type *__
         int4 *dst = (int4 *)sops;
         for (int i = tid; i < d.nops; i += T) dst[i] = src[i];
         if (tid < (unsigned)NR) sdep[tid] = d.dep_hi[tid];
-        for (int i = tid; i < kMaxRegSets; i += T) {
-            unsigned packed = 0;
-            for (int k = 0; k < RL; ++k) packed |= (unsigned)d.rb[i][k] << (5 * k);
-            sset[2 * i] = packed;
-            sset[2 * i + 1] = d.tbmask[i];
-        }
+        copy_sets(sset, d.sets, d.nsets, tid, T);
         const R *mats = mats_all + (size_t)b * d.nmats * 8;
         for (int i = tid; i < 8 * d.nmats; i += T) smat[i] = mats[i];
         if (MODE == 1)
@@ -130,11 +130,11 @@ k_adj_stage(typename CT<R>::type *__restrict__ psi_all, typename CT<R>::type *__
                 }
                 __syncthreads();
             }
-            const unsigned packed = sset[2 * o.reg];
-            e0 = pdep_sw(tid, sset[2 * o.reg + 1]);
-            P0 = Swz<R>::f(e0);
+            const SetSlots &ss = sset[o.reg];
+            P0 = (unsigned)ss.lo[tid & 31u] ^ (unsigned)ss.hi[tid >> 5];
+            e0 = Swz<R>::f(P0);
 #pragma unroll
-            for (int k = 0; k < RL; ++k) q[k] = Swz<R>::f(1u << ((packed >> (5 * k)) & 31u));
+            for (int k = 0; k < RL; ++k) q[k] = ss.q[k];
 #pragma unroll
             for (int j = 0; j < NR; ++j) {
                 unsigned sl_ = reg_slot<RL>(P0, q, j);
@@ -312,7 +312,7 @@ void adj_dispatch(void *psi, void *lam, const AdjStageDesc &d, const void *mats,
     typedef typename CT<R>::type C;
     const int NRmax = 1 << d.rl;
     size_t smem = ((size_t)sizeof(C) << d.m) * (MODE == 1 ? 2 : 1) + (size_t)d.nops * sizeof(AdjOp) +
-                  sizeof(long long) * NRmax + sizeof(unsigned) * 2 * kMaxRegSets +
+                  sizeof(long long) * NRmax + adj_sets_bytes(d.nsets) +
                   sizeof(R) * (8 * (size_t)d.nmats + (size_t)d.ngrads);
     idx_t tiles = (idx_t)1 << (d.n - d.m);
     int threads = 1 << (d.m - d.rl);

@@ -197,12 +197,8 @@ bool schedule(const std::vector<Op> &ops, const std::vector<int> &idxs, unsigned
         for (int b = 0; b < m && (int)want.size() < rl; ++b)
             if (std::find(want.begin(), want.end(), b) == want.end()) want.push_back(b);
         if (nsets >= kMaxRegSets || d.nops >= kMaxAdjOps) return false;
-        unsigned mask = 0;
-        for (int k = 0; k < rl; ++k) {
-            d.rb[nsets][k] = (unsigned char)want[k];
-            mask |= 1u << want[k];
-        }
-        d.tbmask[nsets] = (unsigned short)(((1u << m) - 1) & ~mask);
+        d.sets[nsets] = make_set_slots(want.data(), rl, m, sizeof(R) == 4 ? kFP32 : kFP64);
+        d.nsets = nsets + 1;
         AdjOp &o = d.ops[d.nops++];
         memset(&o, 0, sizeof(o));
         o.kind = kOpTranspose;

@@ -477,15 +477,11 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
     d.rl = rl;
     fill_tile_header(tl, n, rl, d.lowrun, d.nhi, d.hi_pos, d.nins, d.ins_pos, d.dep_hi);
     d.nops = (int)ops.size();
+    d.nsets = (int)sets.size();
     for (int i = 0; i < d.nops; ++i) d.ops[i] = ops[i];
-    for (size_t si = 0; si < sets.size(); ++si) {
-        unsigned mask = 0;
-        for (int k = 0; k < rl; ++k) {
-            d.rb[si][k] = (unsigned char)sets[si][k];
-            mask |= 1u << sets[si][k];
-        }
-        d.tbmask[si] = (unsigned short)(((1u << m) - 1) & ~mask);
-    }
+    const int prec = sizeof(R) == 4 ? kFP32 : kFP64;
+    for (size_t si = 0; si < sets.size(); ++si)
+        d.sets[si] = make_set_slots(sets[si].data(), rl, m, prec);
     return true;
 }
 
@@ -1356,16 +1352,8 @@ plan_gate_stages(const std::vector<PendingGate> &gates, int n, int M, int low) {
 }
 
 static void append_sets(const std::vector<std::vector<int>> &sets, int m, int rl,
-                        std::vector<unsigned> &sets_all) {
-    for (auto &st : sets) {
-        unsigned packed = 0, mask = 0;
-        for (int k = 0; k < rl; ++k) {
-            packed |= (unsigned)st[k] << (5 * k);
-            mask |= 1u << st[k];
-        }
-        sets_all.push_back(packed);
-        sets_all.push_back(((1u << m) - 1) & ~mask);
-    }
+                        std::vector<SetSlots> &sets_all) {
+    for (auto &st : sets) sets_all.push_back(make_set_slots(st.data(), rl, m, kFP32));
 }
 
 int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
@@ -1374,84 +1362,127 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
     if (prec != kFP32) fail(QG_ERR_VALUE, "batched circuits run in complex64.");
     if (n_circuits < 1) fail(QG_ERR_VALUE, "no circuits.");
     Device &d = dev();
+    // Plan every circuit independently (in parallel), then concatenate.
+    struct StagePart {
+        BatchStage hdr;  // ops_off / sets_off local to the circuit
+    };
+    struct Plan {
+        int n = 0, rl = 0;
+        bool resident = false;
+        std::vector<RegOp<float>> ops;
+        std::vector<SetSlots> sets;
+        std::vector<StagePart> stages;
+        std::string error;
+    };
+    std::vector<Plan> plans(n_circuits);
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int c = 0; c < n_circuits; ++c) {
+        Plan &P = plans[c];
+        try {
+            const int n = n_qubits[c];
+            P.n = n;
+            if (n < 8 || n > 30) fail(QG_ERR_VALUE, "circuit %d: 8..30 qubits supported.", c);
+            std::vector<PendingGate> gl;
+            for (int64_t gi = gate_offsets[c]; gi < gate_offsets[c + 1]; ++gi) {
+                const qg_circuit_op &op = gates[gi];
+                if (op.kind != 0) fail(QG_ERR_VALUE, "circuit %d: fixed gates only.", c);
+                if (op.target < 0 || op.target >= n || op.n_controls < 0 || op.n_controls > 4)
+                    fail(QG_ERR_VALUE, "circuit %d: bad gate.", c);
+                PendingGate g;
+                g.target = op.target;
+                unsigned long long seen = 1ULL << op.target;
+                for (int k = 0; k < op.n_controls; ++k) {
+                    int q = op.controls[k];
+                    if (q < 0 || q >= n || (seen & (1ULL << q)))
+                        fail(QG_ERR_VALUE, "circuit %d: bad control.", c);
+                    seen |= 1ULL << q;
+                    g.controls.push_back(q);
+                }
+                memcpy(g.m.v, op.mat, sizeof(g.m.v));
+                g.diag = is_diag(g.m);
+                gl.push_back(g);
+            }
+            merge_runs(gl);
+            std::vector<RegOp<float>> prog;
+            std::vector<std::vector<int>> sets;
+            if (n <= 13) {
+                P.resident = true;
+                P.rl = n <= 9 ? 3 : (n <= 12 ? 4 : 5);
+                std::vector<const PendingGate *> ptrs;
+                for (auto &g : gl) ptrs.push_back(&g);
+                TileLanes tl = tile_lanes_of((1ULL << n) - 1, n);
+                build_program<float>(ptrs, tl, P.rl, prog, sets);
+                if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: program too long.", c);
+                P.ops = prog;
+                append_sets(sets, n, P.rl, P.sets);
+            } else {
+                P.rl = 4;
+                auto plan = plan_gate_stages(gl, n, 12, 4);
+                for (size_t r = 0; r < plan.size(); ++r) {
+                    TileLanes tl = tile_lanes_of(plan[r].first, n);
+                    build_program<float>(plan[r].second, tl, 4, prog, sets);
+                    if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: stage too long.", c);
+                    StagePart sp;
+                    memset(&sp.hdr, 0, sizeof(sp.hdr));
+                    sp.hdr.n = n;
+                    sp.hdr.m = 12;
+                    sp.hdr.rl = 4;
+                    fill_tile_header(tl, n, 4, sp.hdr.lowrun, sp.hdr.nhi, sp.hdr.hi_pos,
+                                     sp.hdr.nins, sp.hdr.ins_pos, sp.hdr.dep_hi);
+                    sp.hdr.nops = (int)prog.size();
+                    sp.hdr.ops_off = (long long)P.ops.size();
+                    sp.hdr.sets_off = (int)P.sets.size();
+                    P.ops.insert(P.ops.end(), prog.begin(), prog.end());
+                    append_sets(sets, 12, 4, P.sets);
+                    P.stages.push_back(sp);
+                }
+            }
+        } catch (const Error &e) {
+            P.error = e.msg.empty() ? "planning failed" : e.msg;
+        } catch (...) {
+            P.error = "planning failed";
+        }
+    }
+    for (auto &P : plans)
+        if (!P.error.empty()) fail(QG_ERR_VALUE, "%s", P.error.c_str());
+
     std::vector<RegOp<float>> ops_all;
-    std::vector<unsigned> sets_all;
+    std::vector<SetSlots> sets_all;
     std::vector<ResidentCircuit> res[14];
     std::vector<BatchStage> stages;
     std::vector<std::vector<int2>> rounds;
     std::vector<long long> big_off;
     std::vector<int> big_n, big_idx;
     long long arena_elems = 0;
-    std::vector<RegOp<float>> prog;
-    std::vector<std::vector<int>> sets;
     for (int c = 0; c < n_circuits; ++c) {
-        const int n = n_qubits[c];
-        if (n < 8 || n > 30) fail(QG_ERR_VALUE, "circuit %d: 8..30 qubits supported.", c);
-        std::vector<PendingGate> gl;
-        for (int64_t gi = gate_offsets[c]; gi < gate_offsets[c + 1]; ++gi) {
-            const qg_circuit_op &op = gates[gi];
-            if (op.kind != 0) fail(QG_ERR_VALUE, "circuit %d: fixed gates only.", c);
-            if (op.target < 0 || op.target >= n || op.n_controls < 0 || op.n_controls > 4)
-                fail(QG_ERR_VALUE, "circuit %d: bad gate.", c);
-            PendingGate g;
-            g.target = op.target;
-            unsigned long long seen = 1ULL << op.target;
-            for (int k = 0; k < op.n_controls; ++k) {
-                int q = op.controls[k];
-                if (q < 0 || q >= n || (seen & (1ULL << q)))
-                    fail(QG_ERR_VALUE, "circuit %d: bad control.", c);
-                seen |= 1ULL << q;
-                g.controls.push_back(q);
-            }
-            memcpy(g.m.v, op.mat, sizeof(g.m.v));
-            g.diag = is_diag(g.m);
-            gl.push_back(g);
-        }
-        merge_runs(gl);
-        if (n <= 13) {
-            const int rl = n <= 9 ? 3 : (n <= 12 ? 4 : 5);
-            std::vector<const PendingGate *> ptrs;
-            for (auto &g : gl) ptrs.push_back(&g);
-            TileLanes tl = tile_lanes_of(n >= 64 ? ~0ULL : ((1ULL << n) - 1), n);
-            build_program<float>(ptrs, tl, rl, prog, sets);
-            if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: program too long.", c);
+        Plan &P = plans[c];
+        const long long ops_base = (long long)ops_all.size();
+        const int sets_base = (int)sets_all.size();
+        ops_all.insert(ops_all.end(), P.ops.begin(), P.ops.end());
+        sets_all.insert(sets_all.end(), P.sets.begin(), P.sets.end());
+        if (P.resident) {
             ResidentCircuit rc;
-            rc.ops_off = (long long)ops_all.size();
-            rc.nops = (int)prog.size();
-            rc.sets_off = (int)(sets_all.size() / 2);
+            rc.ops_off = ops_base;
+            rc.nops = (int)P.ops.size();
+            rc.sets_off = sets_base;
             rc.out_index = c;
             rc.pad = 0;
-            ops_all.insert(ops_all.end(), prog.begin(), prog.end());
-            append_sets(sets, n, rl, sets_all);
-            res[n].push_back(rc);
+            res[P.n].push_back(rc);
         } else {
             const long long off = arena_elems;
-            arena_elems += ((1LL << n) + 31) & ~31LL;
+            arena_elems += ((1LL << P.n) + 31) & ~31LL;
             big_off.push_back(off);
-            big_n.push_back(n);
+            big_n.push_back(P.n);
             big_idx.push_back(c);
-            auto plan = plan_gate_stages(gl, n, 12, 4);
-            for (size_t r = 0; r < plan.size(); ++r) {
-                TileLanes tl = tile_lanes_of(plan[r].first, n);
-                build_program<float>(plan[r].second, tl, 4, prog, sets);
-                if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: stage too long.", c);
-                BatchStage st;
-                memset(&st, 0, sizeof(st));
+            for (size_t r = 0; r < P.stages.size(); ++r) {
+                BatchStage st = P.stages[r].hdr;
                 st.state_off = off;
-                st.n = n;
-                st.m = 12;
-                st.rl = 4;
-                fill_tile_header(tl, n, 4, st.lowrun, st.nhi, st.hi_pos, st.nins, st.ins_pos,
-                                 st.dep_hi);
-                st.nops = (int)prog.size();
-                st.ops_off = (long long)ops_all.size();
-                st.sets_off = (int)(sets_all.size() / 2);
-                ops_all.insert(ops_all.end(), prog.begin(), prog.end());
-                append_sets(sets, 12, 4, sets_all);
+                st.ops_off += ops_base;
+                st.sets_off += sets_base;
                 int sidx = (int)stages.size();
                 stages.push_back(st);
                 if (rounds.size() <= r) rounds.resize(r + 1);
-                for (long long t = 0; t < (1LL << (n - 12)); ++t)
+                for (long long t = 0; t < (1LL << (P.n - 12)); ++t)
                     rounds[r].push_back(make_int2(sidx, (int)t));
             }
         }
@@ -1467,7 +1498,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
     cudaGraphExec_t exec = nullptr;
     try {
         auto *d_ops = (RegOp<float> *)up(ops_all.data(), ops_all.size() * sizeof(RegOp<float>));
-        auto *d_sets = (unsigned *)up(sets_all.data(), sets_all.size() * sizeof(unsigned));
+        auto *d_sets = (SetSlots *)up(sets_all.data(), sets_all.size() * sizeof(SetSlots));
         ResidentCircuit *d_res[14];
         for (int n = 8; n <= 13; ++n)
             d_res[n] = (ResidentCircuit *)up(res[n].data(), res[n].size() * sizeof(ResidentCircuit));

@@ -21,12 +21,12 @@ using namespace rs;
 typedef float R;
 typedef float2 C;
 
-// Runs ops[0..nops) on the register-resident tile.  `sets` holds 2 words per
-// register set (packed 5-bit lanes, thread-lane mask).  On return, a[] holds
-// the thread's amplitudes for register set (rbl, P0, q, e0).
+// Runs ops[0..nops) on the register-resident tile; `sets` are the slot
+// tables of the program's register sets.  On return, a[] holds the thread's
+// amplitudes for the last register set (e0, P0, q; lanebit[k] = its lanes).
 template <int RL>
 __device__ __forceinline__ void run_program(C (&a)[1 << RL], C *sm, const RegOp<R> *ops, int nops,
-                                            const unsigned *sets, unsigned tid, unsigned &e0,
+                                            const SetSlots *sets, unsigned tid, unsigned &e0,
                                             unsigned &P0, unsigned (&q)[RL],
                                             unsigned (&lanebit)[RL]) {
     constexpr int NR = 1 << RL;
@@ -39,13 +39,13 @@ __device__ __forceinline__ void run_program(C (&a)[1 << RL], C *sm, const RegOp<
                 for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
                 __syncthreads();
             }
-            const unsigned packed = sets[2 * o.reg];
-            e0 = pdep_sw(tid, sets[2 * o.reg + 1]);
-            P0 = Swz<R>::f(e0);
+            const SetSlots &ss = sets[o.reg];
+            P0 = (unsigned)ss.lo[tid & 31u] ^ (unsigned)ss.hi[tid >> 5];
+            e0 = Swz<R>::f(P0);
 #pragma unroll
             for (int k = 0; k < RL; ++k) {
-                lanebit[k] = 1u << ((packed >> (5 * k)) & 31u);
-                q[k] = Swz<R>::f(lanebit[k]);
+                q[k] = ss.q[k];
+                lanebit[k] = Swz<R>::f(q[k]);
             }
 #pragma unroll
             for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
@@ -87,7 +87,7 @@ __device__ __forceinline__ double block_sum_d(double v, double *ws) {
 template <int RL>
 __global__ void __launch_bounds__(512)
 k_batch_resident(int n, const ResidentCircuit *__restrict__ circuits,
-                 const RegOp<R> *__restrict__ ops_all, const unsigned *__restrict__ sets_all,
+                 const RegOp<R> *__restrict__ ops_all, const SetSlots *__restrict__ sets_all,
                  double *__restrict__ out) {
     constexpr int NR = 1 << RL;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -104,7 +104,7 @@ k_batch_resident(int n, const ResidentCircuit *__restrict__ circuits,
     unsigned e0 = 0, P0 = 0, q[RL], lanebit[RL];
 #pragma unroll
     for (int k = 0; k < RL; ++k) q[k] = lanebit[k] = 0;
-    run_program<RL>(a, sm, ops_all + c.ops_off, c.nops, sets_all + 2 * c.sets_off, tid, e0, P0, q,
+    run_program<RL>(a, sm, ops_all + c.ops_off, c.nops, sets_all + c.sets_off, tid, e0, P0, q,
                     lanebit);
     // sum_i <Z_i> = sum_b |psi_b|^2 (n - 2 popcount(b))
     float part = 0.f;
@@ -124,7 +124,7 @@ k_batch_resident(int n, const ResidentCircuit *__restrict__ circuits,
 // 16 per thread in registers (256 threads).
 __global__ void __launch_bounds__(256)
 k_batch_stage(const BatchStage *__restrict__ stages, const int2 *__restrict__ items,
-              const RegOp<R> *__restrict__ ops_all, const unsigned *__restrict__ sets_all,
+              const RegOp<R> *__restrict__ ops_all, const SetSlots *__restrict__ sets_all,
               C *__restrict__ arena) {
     constexpr int RL = 4, NR = 16;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -151,7 +151,7 @@ k_batch_stage(const BatchStage *__restrict__ stages, const int2 *__restrict__ it
     unsigned e0 = 0, P0 = 0, q[RL], lanebit[RL];
 #pragma unroll
     for (int k = 0; k < RL; ++k) q[k] = lanebit[k] = 0;
-    run_program<RL>(a, sm, ops_all + st.ops_off, st.nops, sets_all + 2 * st.sets_off, tid, e0, P0,
+    run_program<RL>(a, sm, ops_all + st.ops_off, st.nops, sets_all + st.sets_off, tid, e0, P0,
                     q, lanebit);
     __syncthreads();
 #pragma unroll
@@ -209,7 +209,7 @@ __global__ void k_batch_init(C *arena, const long long *__restrict__ off, int co
 }  // namespace
 
 void launch_batch_resident(int n, int rl, const ResidentCircuit *d_circuits, int count,
-                           const RegOp<float> *d_ops, const unsigned *d_sets, double *d_out,
+                           const RegOp<float> *d_ops, const SetSlots *d_sets, double *d_out,
                            cudaStream_t stream) {
     if (count <= 0) return;
     size_t smem = sizeof(C) << n;
@@ -227,7 +227,7 @@ void launch_batch_resident(int n, int rl, const ResidentCircuit *d_circuits, int
 }
 
 void launch_batch_stage(const BatchStage *d_stages, const int2 *d_items, int n_items,
-                        const RegOp<float> *d_ops, const unsigned *d_sets, float2 *arena,
+                        const RegOp<float> *d_ops, const SetSlots *d_sets, float2 *arena,
                         cudaStream_t stream) {
     if (n_items <= 0) return;
     size_t smem = sizeof(C) << 12;

@@ -116,7 +116,7 @@ k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDes
     C *sm = (C *)smraw;
     Op *sops = (Op *)(smraw + ((size_t)sizeof(C) << m));
     long long *sdep = (long long *)(sops + d.nops);
-    unsigned *sset = (unsigned *)(sdep + NR);  // per set: rb lanes packed 5x5 bits, tbmask
+    SetSlots *sset = (SetSlots *)(sdep + NR);
     const unsigned tid = threadIdx.x;
 
     {
@@ -125,12 +125,7 @@ k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDes
         const int nvec = (int)(d.nops * sizeof(Op) / sizeof(int4));
         for (int i = tid; i < nvec; i += T) dst[i] = src[i];
         if (tid < (unsigned)NR) sdep[tid] = d.dep_hi[tid];
-        for (int i = tid; i < kMaxRegSets; i += T) {
-            unsigned packed = 0;
-            for (int k = 0; k < RL; ++k) packed |= (unsigned)d.rb[i][k] << (5 * k);
-            sset[2 * i] = packed;
-            sset[2 * i + 1] = d.tbmask[i];
-        }
+        copy_sets(sset, d.sets, d.nsets, tid, T);
     }
     const idx_t base = insert_zeros((idx_t)blockIdx.x, d.ins_pos, d.nins);
     // Global offset of tile element tid (tile lanes 0..t-1); the offsets of
@@ -166,11 +161,11 @@ k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDes
                 for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
                 __syncthreads();
             }
-            const unsigned packed = sset[2 * o.reg];
-            e0 = pdep_sw(tid, sset[2 * o.reg + 1]);
-            P0 = Swz<R>::f(e0);
+            const SetSlots &ss = sset[o.reg];
+            P0 = (unsigned)ss.lo[tid & 31u] ^ (unsigned)ss.hi[tid >> 5];
+            e0 = Swz<R>::f(P0);  // the swizzle is an involution
 #pragma unroll
-            for (int k = 0; k < RL; ++k) q[k] = Swz<R>::f(1u << ((packed >> (5 * k)) & 31u));
+            for (int k = 0; k < RL; ++k) q[k] = ss.q[k];
 #pragma unroll
             for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
             continue;
@@ -224,20 +219,16 @@ k_rstage_pipe(typename CT<R>::type *__restrict__ s, const __grid_constant__ RSta
     C *buf1 = buf0 + (1 << m);
     Op *sops = (Op *)(smraw + ((size_t)sizeof(C) << (m + 1)));
     long long *sdep = (long long *)(sops + d.nops);
-    unsigned *sset = (unsigned *)(sdep + NR);
+    SetSlots *sset = (SetSlots *)(sdep + NR);
     const unsigned tid = threadIdx.x;
+
     {
         const int4 *src = (const int4 *)d.ops;
         int4 *dst = (int4 *)sops;
         const int nvec = (int)(d.nops * sizeof(Op) / sizeof(int4));
         for (int i = tid; i < nvec; i += T) dst[i] = src[i];
         if (tid < (unsigned)NR) sdep[tid] = d.dep_hi[tid];
-        for (int i = tid; i < kMaxRegSets; i += T) {
-            unsigned packed = 0;
-            for (int k = 0; k < RL; ++k) packed |= (unsigned)d.rb[i][k] << (5 * k);
-            sset[2 * i] = packed;
-            sset[2 * i + 1] = d.tbmask[i];
-        }
+        copy_sets(sset, d.sets, d.nsets, tid, T);
     }
     const int lr = d.lowrun < t ? d.lowrun : t;
     idx_t dt = (idx_t)(tid & ((1u << lr) - 1u));
@@ -283,12 +274,11 @@ k_rstage_pipe(typename CT<R>::type *__restrict__ s, const __grid_constant__ RSta
                     for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
                     __syncthreads();
                 }
-                const unsigned packed = sset[2 * o.reg];
-                e0 = pdep_sw(tid, sset[2 * o.reg + 1]);
-                P0 = Swz<R>::f(e0);
+                const SetSlots &ss = sset[o.reg];
+                P0 = (unsigned)ss.lo[tid & 31u] ^ (unsigned)ss.hi[tid >> 5];
+                e0 = Swz<R>::f(P0);
 #pragma unroll
-                for (int kk = 0; kk < RL; ++kk)
-                    q[kk] = Swz<R>::f(1u << ((packed >> (5 * kk)) & 31u));
+                for (int kk = 0; kk < RL; ++kk) q[kk] = ss.q[kk];
 #pragma unroll
                 for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
                 continue;
@@ -328,7 +318,7 @@ template <class R>
 void rstage_dispatch(void *state, const RStageDesc<R> &d, cudaStream_t stream, bool pipelined) {
     typedef typename CT<R>::type C;
     const size_t prog = (size_t)d.nops * sizeof(RegOp<R>) + sizeof(long long) * (1 << d.rl) +
-                        sizeof(unsigned) * 2 * kMaxRegSets;
+                        sizeof(SetSlots) * (size_t)d.nsets;
     const size_t tile_bytes = ((size_t)1 << d.m) * sizeof(C);
     idx_t tiles = (idx_t)1 << (d.n - d.m);
     int threads = 1 << (d.m - d.rl);

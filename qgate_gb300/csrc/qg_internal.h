@@ -111,6 +111,15 @@ template <class R> struct alignas(16) RegOp {
 static_assert(sizeof(RegOp<float>) == 48, "RegOp<float> layout");
 static_assert(sizeof(RegOp<double>) == 80, "RegOp<double> layout");
 
+// Shared-memory slot tables of one register set (host-precomputed): the
+// swizzled slot of a thread's element 0 is lo[tid & 31] ^ hi[tid >> 5];
+// register j adds the XOR of q[k] over the set bits k of j.
+struct SetSlots {
+    unsigned short lo[32];
+    unsigned short hi[16];
+    unsigned short q[kMaxRegLanes + 1];
+};
+
 template <class R> struct RStageDesc {
     int n, m, rl;              // lanes of the state, tile lanes, register lanes
     int lowrun, nhi;
@@ -118,11 +127,36 @@ template <class R> struct RStageDesc {
     int nins;
     int ins_pos[kMaxTileLanes];
     long long dep_hi[1 << kMaxRegLanes];  // global offset of tile element (i << (m - rl))
-    int nops;
-    unsigned char rb[kMaxRegSets][kMaxRegLanes];  // register set -> tile lanes
-    unsigned short tbmask[kMaxRegSets];           // its complement (thread lanes)
+    int nops, nsets;
+    // Per register set: the swizzled shared-memory slot of the thread's
+    // element 0 is slot_lo[tid & 31] ^ slot_hi[tid >> 5] (the bit deposit of
+    // the thread index into the thread lanes, and the swizzle, are both
+    // linear over GF(2)), and register j adds the XOR of slot_q[k] over the
+    // set bits k of j.  Precomputed on the host.
+    SetSlots sets[kMaxRegSets];
     RegOp<R> ops[kMaxRegOps];                     // 16-byte aligned
 };
+
+// XOR swizzle of shared-memory element slots (see qg_regstage.cuh):
+// 16 slots per 128-byte row for complex64, 8 for complex128.  An involution.
+inline unsigned host_swz(unsigned e, int prec);
+inline unsigned host_pdep(unsigned x, unsigned mask);
+// Slot tables of a register set with tile lanes rb[0..rl) in an m-lane tile.
+inline SetSlots make_set_slots(const int *rb, int rl, int m, int prec);
+
+inline unsigned host_swz(unsigned e, int prec) {
+    return prec == kFP32 ? e ^ (((e >> 4) ^ (e >> 8) ^ (e >> 12)) & 15u)
+                         : e ^ (((e >> 3) ^ (e >> 6) ^ (e >> 9) ^ (e >> 12)) & 7u);
+}
+inline unsigned host_pdep(unsigned x, unsigned mask) {
+    unsigned r = 0;
+    for (unsigned b = 1; mask; b <<= 1) {
+        unsigned low = mask & (0u - mask);
+        if (x & b) r |= low;
+        mask &= mask - 1;
+    }
+    return r;
+}
 
 // pipelined: persistent grid with double-buffered tiles (when the state has
 // enough tiles and two fit in shared memory).
@@ -158,9 +192,8 @@ struct AdjStageDesc {
     int nins;
     int ins_pos[kMaxTileLanes];
     long long dep_hi[1 << kMaxRegLanes];
-    int nops, nmats, ngrads;
-    unsigned char rb[kMaxRegSets][kMaxRegLanes];
-    unsigned short tbmask[kMaxRegSets];
+    int nops, nmats, ngrads, nsets;
+    SetSlots sets[kMaxRegSets];
     AdjOp ops[kMaxAdjOps];
 };
 
@@ -211,12 +244,12 @@ struct ResidentCircuit {
 };
 
 void launch_batch_resident(int n, int rl, const ResidentCircuit *d_circuits, int count,
-                           const RegOp<float> *d_ops, const unsigned *d_sets, double *d_out,
+                           const RegOp<float> *d_ops, const SetSlots *d_sets, double *d_out,
                            cudaStream_t stream);
 // One round: every (stage, tile) work item of the round.  d_items[i] =
 // {stage index, tile index}.
 void launch_batch_stage(const BatchStage *d_stages, const int2 *d_items, int n_items,
-                        const RegOp<float> *d_ops, const unsigned *d_sets, float2 *arena,
+                        const RegOp<float> *d_ops, const SetSlots *d_sets, float2 *arena,
                         cudaStream_t stream);
 // out[out_index[c]] = sum_i <Z_i> over 2^n_c amplitudes at arena + off[c];
 // FP64; d_partials holds batch_sumz_partials(count) doubles.
@@ -292,4 +325,26 @@ void launch_scan_apply(double *data, idx_t n, double *d_scratch, double norm,
 void launch_search(const double *cdf, idx_t n, const double *u, long long *obs, idx_t n_samples,
                    const int *empty_pos, int n_empty, cudaStream_t stream);
 
+inline SetSlots make_set_slots(const int *rb, int rl, int m, int prec) {
+    SetSlots ss;
+    for (auto &v : ss.q) v = 0;
+    unsigned mask = 0;
+    for (int k = 0; k < rl; ++k) {
+        mask |= 1u << rb[k];
+        ss.q[k] = (unsigned short)host_swz(1u << rb[k], prec);
+    }
+    const unsigned tb = ((1u << m) - 1) & ~mask;
+    for (unsigned x = 0; x < 32; ++x) ss.lo[x] = (unsigned short)host_swz(host_pdep(x, tb), prec);
+    for (unsigned x = 0; x < 16; ++x)
+        ss.hi[x] = (unsigned short)host_swz(host_pdep(x << 5, tb), prec);
+    return ss;
+}
+
+}  // namespace qg
+
+namespace qg {
+// Kernel parameters are limited to 32764 bytes (CUDA 12.1+).
+static_assert(sizeof(RStageDesc<double>) + 16 <= 32764, "stage descriptor too large");
+static_assert(sizeof(AdjStageDesc) + 64 <= 32764, "adjoint descriptor too large");
+static_assert(sizeof(StageDesc) + 16 <= 32764, "stage descriptor too large");
 }  // namespace qg

@@ -42,6 +42,15 @@ template <class C> __device__ __forceinline__ void cp_async_elem(C *smem, const 
 }
 
 // Shared-memory slot of register j: P0 ^ (XOR of q[k] over the set bits k of j).
+__device__ __forceinline__ void copy_sets(SetSlots *dst, const SetSlots *src, int nsets,
+                                          unsigned tid, unsigned T) {
+    static_assert(sizeof(SetSlots) % 4 == 0, "SetSlots size");
+    const unsigned *s = (const unsigned *)src;
+    unsigned *d = (unsigned *)dst;
+    const int words = nsets * (int)(sizeof(SetSlots) / 4);
+    for (int i = tid; i < words; i += T) d[i] = s[i];
+}
+
 template <int RL>
 __device__ __forceinline__ unsigned reg_slot(unsigned P0, const unsigned (&q)[RL], int j) {
     unsigned a = P0;
