@@ -149,6 +149,16 @@ int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budge
  * stage kernel; 0 (default) with one CTA per tile, which keeps more warps
  * resident per SM. */
 int qg_set_stage_pipelining(int on);
+/* Extension: 1 runs complex64 stages of 12- or 13-lane tiles as fused 5-lane
+ * blocks (32x32 complex matrices) on the tensor cores, 0 (default) on the
+ * register-resident CUDA-core stage kernel.  No reference counterpart: the
+ * reference applies one gate per pass
+ * (qgate/simulator/src/CUDAQubitProcessor.cpp:271, applyGate). */
+int qg_set_tensor_blocks(int on);
+/* Extension: status word of the tensor-core stage kernels after a
+ * synchronize: 0 = every bounded wait completed; nonzero = a wait gave up
+ * (that stage's tiles were left unchanged).  reset != 0 clears it. */
+int qg_tensor_stage_status(int reset, int *status);
 /* Extension: counters of the gate path since the last reset
  * {gates, passes, bytes_moved}. */
 int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset);

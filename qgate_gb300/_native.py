@@ -55,6 +55,8 @@ SIGNATURES = {
     'qg_set_fusion': [_i],
     'qg_set_fusion_params': [_i, _i, _i, _i],
     'qg_set_stage_pipelining': [_i],
+    'qg_set_tensor_blocks': [_i],
+    'qg_tensor_stage_status': [_i, _ip],
     'qg_gate_stats': [_i64p, _i64p, _i64p, _i],
     'qg_timing_enable': [_i],
     'qg_timing_read': [ctypes.c_char_p, _i64p, _dp, _i],
@@ -151,6 +153,18 @@ def set_fusion_params(prec, tile_lanes, reg_lanes, cost_budget=0):
     call('qg_set_fusion_params', int(prec), int(tile_lanes), int(reg_lanes), int(cost_budget))
 
 
+def set_tensor_blocks(on):
+    """Run complex64 stages of 12/13-lane tiles as fused 5-lane blocks on the
+    tensor cores (tcgen05, 3xTF32)."""
+    call('qg_set_tensor_blocks', 1 if on else 0)
+
+
+def tensor_stage_status(reset=False):
+    v = ctypes.c_int(0)
+    check(lib.qg_tensor_stage_status(1 if reset else 0, ctypes.byref(v)))
+    return v.value
+
+
 def gate_stats(reset=False):
     g, p, b = _i64(0), _i64(0), _i64(0)
     check(lib.qg_gate_stats(ctypes.byref(g), ctypes.byref(p), ctypes.byref(b), 1 if reset else 0))
@@ -168,7 +182,7 @@ def timing_read(kernel_class, reset=False):
     return n.value, ms.value
 
 
-KERNEL_CLASSES = ('stage', 'gate', 'multi', 'init', 'prob', 'pauli', 'measure', 'join',
+KERNEL_CLASSES = ('stage', 'tstage', 'gate', 'multi', 'init', 'prob', 'pauli', 'measure', 'join',
                   'gather', 'marginal', 'scan', 'search', 'batch')
 
 

@@ -154,6 +154,13 @@ struct Device {
     int reg_lanes[3] = {0, 4, 4};
     int cost_budget[3] = {0, 0, 0};
     bool pipelined = false;  // persistent double-buffered stage kernel (opt-in)
+    // complex64 stages on 12- or 13-lane tiles as fused 5-lane blocks on the
+    // tensor cores (opt-in; the autotuner may select it).
+    bool tensor_blocks = false;
+    // Ring of split block operands: pinned host staging and its device copy.
+    static constexpr size_t kBRingBytes = 32ull << 20;
+    unsigned short *h_bring = nullptr, *d_bring = nullptr;
+    size_t bring_off = 0;
     long long n_gates = 0, n_passes = 0, n_bytes = 0;
     // Per-kernel-class launch timing with CUDA events on the engine's stream.
     bool timing = false;
@@ -485,6 +492,264 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
     return true;
 }
 
+// ------------------------------------------------------------ tensor-core stages
+
+// Register layout of a tile: thread r holds row r (bits i of r at tile
+// positions rows[i]), register pair j holds amplitude j (bits k of j at
+// tile positions amps[k]).
+struct TcLayout {
+    int rows[8];
+    int amps[5];
+};
+
+// Operand layout of a block (tile index -> operand slot; a slot is one
+// complex amplitude as f16x2), a bit permutation: amps[0..1] -> 0..1,
+// rows[0..2] -> 2..4, amps[2] -> 5, rows[3..6] -> 6..9, amps[3..4] ->
+// 10..11, rows[7] -> 12.  Slot bits 0..1 (with the complex part) span one
+// 16-byte core-matrix row along K, rows[0..2] the 8 rows of a core matrix,
+// amps[2] the second core matrix of an MMA's K = 16 (leading byte offset
+// 128), rows[3..6] the 8-row groups (stride byte offset 256), amps[3..4]
+// the K-step (4096 bytes per MMA), rows[7] the second 128-row group (16384
+// bytes).
+static unsigned tc_operand_slot(const TcLayout &L, unsigned tidx) {
+    static const int row_dst[8] = {2, 3, 4, 6, 7, 8, 9, 12};
+    static const int amp_dst[5] = {0, 1, 5, 10, 11};
+    unsigned out = 0;
+    for (int i = 0; i < 8; ++i)
+        if (L.rows[i] >= 0 && (tidx >> L.rows[i] & 1u)) out |= 1u << row_dst[i];
+    for (int k = 0; k < 5; ++k)
+        if (tidx >> L.amps[k] & 1u) out |= 1u << amp_dst[k];
+    return out;
+}
+
+template <class F> static SetSlots tc_slots(const TcLayout &src, int t, F dst) {
+    SetSlots ss;
+    memset(&ss, 0, sizeof(ss));
+    auto dep = [&](unsigned x) {
+        unsigned ti = 0;
+        for (int i = 0; i < t; ++i)
+            if (x >> i & 1u) ti |= 1u << src.rows[i];
+        return ti;
+    };
+    for (unsigned x = 0; x < 32; ++x) ss.lo[x] = (unsigned short)dst(dep(x));
+    for (unsigned x = 0; x < 16 && (x << 5) < (1u << t); ++x)
+        ss.hi[x] = (unsigned short)dst(dep(x << 5));
+    for (int k = 0; k < 5; ++k) ss.q[k] = (unsigned short)dst(1u << src.amps[k]);
+    return ss;
+}
+
+// IEEE binary16 bits of x, rounded to nearest even (subnormals kept).
+static unsigned short f16_bits(float x) {
+    unsigned f;
+    memcpy(&f, &x, 4);
+    const unsigned sign = (f >> 16) & 0x8000u;
+    const int e = (int)((f >> 23) & 0xffu) - 127 + 15;
+    unsigned mant = f & 0x7fffffu;
+    if (e >= 31) return (unsigned short)(sign | 0x7c00u);
+    if (e <= 0) {
+        if (e < -10) return (unsigned short)sign;
+        mant |= 0x800000u;
+        const int shift = 14 - e;
+        unsigned hm = mant >> shift;
+        const unsigned rem = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (hm & 1u))) ++hm;
+        return (unsigned short)(sign | hm);
+    }
+    unsigned out = ((unsigned)e << 10) | (mant >> 13);
+    const unsigned rem = mant & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (out & 1u))) ++out;
+    return (unsigned short)(sign | out);
+}
+
+static double f16_value(unsigned short h) {
+    const int e = (h >> 10) & 31, mant = h & 1023;
+    double v = e == 0 ? std::ldexp((double)mant, -24) : std::ldexp((double)(mant | 1024), e - 25);
+    return (h & 0x8000u) ? -v : v;
+}
+
+// Split operand of a 32x32 complex block U (row-major, amplitude order of
+// the block layout): B[k][n] of D = A B with A[r][2i + c] = (Re, Im) V[r][i]
+// and D[r][2o + c] = (Re, Im) (U V[r])[o], stored K-major (row n holds its
+// K elements) in the canonical no-swizzle layout: element (n, k) at FP16
+// index (k / 16) * 1024 + (k % 16 / 8) * 512 + (n / 8) * 64 + (n % 8) * 8 +
+// k % 8.  Bh = f16(B), Bl = f16(B - Bh), both rounded to nearest.
+static void tc_operand(const std::complex<double> *U, unsigned short *bh, unsigned short *bl) {
+    for (int o = 0; o < 32; ++o)
+        for (int i = 0; i < 32; ++i) {
+            const double re = U[o * 32 + i].real(), im = U[o * 32 + i].imag();
+            const double val[2][2] = {{re, -im}, {im, re}};  // [c_out][c_in]
+            for (int co = 0; co < 2; ++co)
+                for (int ci = 0; ci < 2; ++ci) {
+                    const int n = 2 * o + co, k = 2 * i + ci;
+                    const size_t at = (size_t)(k / 16) * 1024 + (k % 16 / 8) * 512 +
+                                      (n / 8) * 64 + (n % 8) * 8 + k % 8;
+                    const double x = val[co][ci];
+                    const unsigned short h = f16_bits((float)x);
+                    bh[at] = h;
+                    bl[at] = f16_bits((float)(x - f16_value(h)));
+                }
+        }
+}
+
+// Greedy 5-lane blocks over a stage's gates in order: a gate joins the open
+// block when its lanes fit and no earlier deferred gate shares a lane (so it
+// commutes with everything deferred); the rest start the next block.
+static std::vector<std::pair<unsigned, std::vector<const PendingGate *>>>
+tc_blocks(const std::vector<const PendingGate *> &gates, const TileLanes &tl) {
+    std::vector<std::pair<unsigned, std::vector<const PendingGate *>>> out;
+    std::vector<const PendingGate *> rem(gates);
+    while (!rem.empty()) {
+        unsigned L = 0, blocked = 0;
+        std::vector<const PendingGate *> take, keep;
+        for (auto *g : rem) {
+            unsigned q = 1u << tl.local_of[g->target];
+            for (int c : g->controls) q |= 1u << tl.local_of[c];
+            if ((q & blocked) || __builtin_popcount(L | q) > 5) {
+                keep.push_back(g);
+                blocked |= q;
+                continue;
+            }
+            L |= q;
+            take.push_back(g);
+        }
+        out.emplace_back(L, std::move(take));
+        rem.swap(keep);
+    }
+    return out;
+}
+
+// Orders a block's lanes and rows so that the stores into its operand hit
+// distinct banks: the bank of a 4-byte slot is its bits 0..4, which come
+// from amps[0..1] and rows[0..2], and a warp's threads differ in the source
+// layout's rows[0..4] (W); each W lane placed there doubles the banks hit.
+// So amps[0..1] are taken from W first, then rows[0..2]; rows[3..4] are
+// chosen so that the next block can do the same (two of this layout's
+// rows[0..4] among its lanes, three outside).
+static TcLayout tc_choose_layout(unsigned lanes, unsigned next_lanes, const TcLayout &src, int m) {
+    unsigned W = 0;
+    for (int x = 0; x < 5; ++x) W |= 1u << src.rows[x];
+    std::vector<int> L, R;
+    for (int p = 0; p < m; ++p) (lanes >> p & 1u ? L : R).push_back(p);
+    auto in_w = [&](int p) { return (W >> p & 1u) != 0; };
+    std::stable_sort(L.begin(), L.end(), [&](int p, int q) { return in_w(p) && !in_w(q); });
+    // rows[0..2]: W lanes first; among equals, lanes outside the next block.
+    auto nxt = [&](int p) { return (next_lanes >> p & 1u) != 0; };
+    std::stable_sort(R.begin(), R.end(), [&](int p, int q) {
+        if (in_w(p) != in_w(q)) return in_w(p);
+        return !nxt(p) && nxt(q);
+    });
+    TcLayout c;
+    for (int x = 0; x < 8; ++x) c.rows[x] = -1;
+    for (int k = 0; k < 5; ++k) c.amps[k] = L[k];
+    for (int x = 0; x < 3; ++x) c.rows[x] = R[x];
+    int inext = 0;
+    for (int x = 0; x < 3; ++x) inext += nxt(c.rows[x]);
+    std::vector<int> rin, rout;
+    for (size_t x = 3; x < R.size(); ++x) (nxt(R[x]) ? rin : rout).push_back(R[x]);
+    std::vector<int> rest;
+    size_t pi = 0, po = 0;
+    for (int x = 0; x < 2; ++x) {
+        if ((inext < 2 && pi < rin.size()) || po >= rout.size()) {
+            rest.push_back(rin[pi++]);
+            ++inext;
+        } else {
+            rest.push_back(rout[po++]);
+        }
+    }
+    while (pi < rin.size()) rest.push_back(rin[pi++]);
+    while (po < rout.size()) rest.push_back(rout[po++]);
+    for (size_t x = 0; x < rest.size(); ++x) c.rows[3 + x] = rest[x];
+    return c;
+}
+
+// U (32x32, row-major) of a block's gates in the amplitude order of `lay`.
+static void tc_block_matrix(const std::vector<const PendingGate *> &gates, const TileLanes &tl,
+                            const TcLayout &lay, std::complex<double> *U) {
+    typedef std::complex<double> cd;
+    int bit_of[64];
+    for (int p = 0; p < 64; ++p) bit_of[p] = -1;
+    for (int k = 0; k < 5; ++k) bit_of[lay.amps[k]] = k;
+    for (int i = 0; i < 1024; ++i) U[i] = (i / 32 == i % 32) ? cd(1, 0) : cd(0, 0);
+    for (auto *g : gates) {
+        const int tb = 1 << bit_of[tl.local_of[g->target]];
+        int cm = 0;
+        for (int c : g->controls) cm |= 1 << bit_of[tl.local_of[c]];
+        const cd m00(g->m.v[0], g->m.v[1]), m01(g->m.v[2], g->m.v[3]), m10(g->m.v[4], g->m.v[5]),
+            m11(g->m.v[6], g->m.v[7]);
+        for (int r = 0; r < 32; ++r) {
+            if ((r & tb) || (r & cm) != cm) continue;
+            for (int c = 0; c < 32; ++c) {
+                cd a0 = U[r * 32 + c], a1 = U[(r | tb) * 32 + c];
+                U[r * 32 + c] = m00 * a0 + m01 * a1;
+                U[(r | tb) * 32 + c] = m10 * a0 + m11 * a1;
+            }
+        }
+    }
+}
+
+static void run_tstage(Device &d, States *s, const TileLanes &tl,
+                       const std::vector<const PendingGate *> &gates) {
+    const int n = s->n_lanes;
+    const int m = (int)tl.lanes.size();
+    const int t = m - 5;
+    auto blocks = tc_blocks(gates, tl);
+    if (!d.h_bring) {
+        QG_CUDA(cudaMallocHost(&d.h_bring, Device::kBRingBytes));
+        QG_CUDA(cudaMalloc(&d.d_bring, Device::kBRingBytes));
+        d.bring_off = 0;
+    }
+    const size_t kBlockHalves = 2 * 64 * 64;
+    const size_t per_launch = (size_t)tstage_max_blocks(m);
+    for (size_t b0 = 0; b0 < blocks.size(); b0 += per_launch) {
+        const int nb = (int)std::min<size_t>(per_launch, blocks.size() - b0);
+        const size_t bytes = nb * kBlockHalves * sizeof(unsigned short);
+        if (d.bring_off + bytes > Device::kBRingBytes) {
+            QG_CUDA(cudaStreamSynchronize(d.stream));  // the staging is reused
+            d.bring_off = 0;
+        }
+        unsigned short *hb = d.h_bring + d.bring_off / sizeof(unsigned short);
+        unsigned short *db = d.d_bring + d.bring_off / sizeof(unsigned short);
+        static TcStageDesc desc;
+        memset(&desc, 0, sizeof(desc));
+        desc.n = n;
+        desc.m = m;
+        long long dep[32];
+        fill_tile_header(tl, n, 5, desc.lowrun, desc.nhi, desc.hi_pos, desc.nins, desc.ins_pos,
+                         dep);
+        for (int i = 0; i < 32; ++i) desc.dep_hi[i] = dep[i];
+        desc.nblocks = nb;
+        desc.bmats = db;
+        TcLayout cur;
+        for (int i = 0; i < 8; ++i) cur.rows[i] = i < t ? i : -1;
+        for (int k = 0; k < 5; ++k) cur.amps[k] = t + k;
+        std::complex<double> U[1024];
+        for (int b = 0; b < nb; ++b) {
+            unsigned lanes = blocks[b0 + b].first;
+            // Fill a block of fewer than 5 lanes with lanes of the source
+            // warp bits first (two of them keep its stores conflict-free).
+            for (int x = 0; x < 5 && __builtin_popcount(lanes) < 5; ++x) {
+                unsigned in_warp = 0;
+                for (int y = 0; y < 5; ++y) in_warp += lanes >> cur.rows[y] & 1u;
+                if (in_warp >= 2) break;
+                lanes |= 1u << cur.rows[x];
+            }
+            for (int p = 0; p < m && __builtin_popcount(lanes) < 5; ++p) lanes |= 1u << p;
+            const unsigned next = b + 1 < nb ? blocks[b0 + b + 1].first : 0u;
+            TcLayout lay = tc_choose_layout(lanes, next, cur, m);
+            desc.sets[b] = tc_slots(cur, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); });
+            tc_block_matrix(blocks[b0 + b].second, tl, lay, U);
+            tc_operand(U, hb + b * kBlockHalves, hb + b * kBlockHalves + kBlockHalves / 2);
+            cur = lay;
+        }
+        desc.sets[nb] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
+        QG_CUDA(cudaMemcpyAsync(db, hb, bytes, cudaMemcpyHostToDevice, d.stream));
+        d.bring_off += bytes;
+        timed(d, "tstage", [&] { launch_tstage(s->d, desc, d.stream); });
+        d.n_passes += 1;
+        d.n_bytes += 2 * ((long long)1 << n) * (long long)complex_size(s->prec);
+    }
+}
+
 static void run_stage(Device &d, States *s, unsigned long long S,
                       const std::vector<const PendingGate *> &gates) {
     const int n = s->n_lanes;
@@ -492,6 +757,10 @@ static void run_stage(Device &d, States *s, unsigned long long S,
     const int m = (int)tl.lanes.size();
     // Valid shapes: 32..512 threads (256 with 5 register lanes), 3..5
     // register lanes (complex128 at most 4).
+    if (d.tensor_blocks && s->prec == kFP32 && (m == 12 || m == 13) && n >= m) {
+        run_tstage(d, s, tl, gates);
+        return;
+    }
     const int max_rl = s->prec == kFP64 ? 4 : 5;
     auto max_t = [](int r) { return r >= 5 ? 8 : 9; };
     int rl = std::min(d.reg_lanes[s->prec], max_rl);
@@ -1224,6 +1493,22 @@ int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budge
     g_dev.tile_lanes[prec] = tile_lanes;
     g_dev.reg_lanes[prec] = reg_lanes;
     g_dev.cost_budget[prec] = cost_budget;
+    QG_END
+}
+
+int qg_set_tensor_blocks(int on) {
+    QG_BEGIN
+    flush_all();
+    g_dev.tensor_blocks = on != 0;
+    QG_END
+}
+
+int qg_tensor_stage_status(int reset, int *status) {
+    QG_BEGIN
+    Device &d = dev();
+    flush_all();
+    QG_CUDA(cudaStreamSynchronize(d.stream));
+    *status = tstage_status(reset != 0);
     QG_END
 }
 

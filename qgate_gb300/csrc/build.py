@@ -20,7 +20,7 @@ OBJDIR = os.path.join(PKG, '_build')
 LIB = os.path.join(PKG, 'libqgate_gb300.so')
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-CU_SOURCES = ['gates.cu', 'reduce.cu', 'fused.cu', 'adjoint.cu', 'batch.cu', 'noalloc.cu']
+CU_SOURCES = ['gates.cu', 'reduce.cu', 'fused.cu', 'adjoint.cu', 'batch.cu', 'noalloc.cu', 'tcstage.cu']
 CXX_SOURCES = ['api.cpp', 'adjoint_host.cpp']
 
 

@@ -137,6 +137,30 @@ template <class R> struct RStageDesc {
     RegOp<R> ops[kMaxRegOps];                     // 16-byte aligned
 };
 
+// Tensor-core stage (complex64): fused 5-lane blocks applied as tcgen05
+// products to a tile of m = 12 or 13 lanes.  sets[b] maps the registers of
+// the layout before block b (the load layout for b = 0) to the slots of block
+// b's operand layout; sets[nblocks] maps the last block's layout to the
+// swizzled natural tile.  bmats holds per block the split operands Bh, Bl
+// (2 x 4096 FP16 values, canonical K-major layout).
+constexpr int kMaxTcBlocks = 24;
+struct TcStageDesc {
+    int n, m;
+    int lowrun, nhi;
+    int hi_pos[kMaxTileLanes];
+    int nins;
+    int ins_pos[kMaxTileLanes];
+    long long dep_hi[32];
+    int nblocks;
+    const unsigned short *bmats;
+    SetSlots sets[kMaxTcBlocks + 1];
+};
+void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream);
+// Blocks one tensor-stage launch holds (its operands stay in shared memory).
+int tstage_max_blocks(int m);
+// Status word of the tensor stage kernels (nonzero: a bounded wait gave up).
+int tstage_status(bool reset);
+
 // XOR swizzle of shared-memory element slots (see qg_regstage.cuh):
 // 16 slots per 128-byte row for complex64, 8 for complex128.  An involution.
 inline unsigned host_swz(unsigned e, int prec);
@@ -346,5 +370,6 @@ namespace qg {
 // Kernel parameters are limited to 32764 bytes (CUDA 12.1+).
 static_assert(sizeof(RStageDesc<double>) + 16 <= 32764, "stage descriptor too large");
 static_assert(sizeof(AdjStageDesc) + 64 <= 32764, "adjoint descriptor too large");
+static_assert(sizeof(TcStageDesc) + 16 <= 32764, "tensor stage descriptor too large");
 static_assert(sizeof(StageDesc) + 16 <= 32764, "stage descriptor too large");
 }  // namespace qg

@@ -1,0 +1,390 @@
+// Tensor-core stage kernel (complex64): a tile of m = 12 or 13 lanes stays
+// on chip while a sequence of fused 5-lane blocks, each a 32x32 complex
+// unitary, is applied to it as tcgen05 matrix products.
+//
+// For a block on tile lanes L[0..4] the tile is a 2^(m-5) x 32 complex matrix
+// V (row = the other m-5 lanes, column = the block's amplitude index); the
+// block computes V U^T.  In real form that is D[rows x 64] = A[rows x 64]
+// B[64 x 64] with A[r][2i + c] = (Re, Im) of V[r][i] and B the real 64x64
+// form of U^T: per 128 rows an M=128, N=64, K=64 product, 4 MMAs of K=16 in
+// kind::f16 (FP16 operands, FP32 accumulator).
+//
+// Precision: the state is carried scaled by 2^12 (exact; amplitudes of a
+// normalised state are <= 1, so |A| <= 2^12 stays far below the FP16 range
+// and typical amplitudes sit in its normal range).  Each operand is split
+// into two FP16 parts rounded to nearest, Ah = f16(A), Al = f16(A - Ah),
+// so |A - Ah - Al| <= 2^-24 |A| + 2^-25 (subnormal spacing), the same for B,
+// and D = Ah Bh + Ah Bl + Al Bh in FP32 (the dropped Al Bl term is <= 2^-24
+// relative): about FP32 accuracy per block.
+//
+// Data path per block: thread r holds row r of the previous layout in
+// registers (64 floats); it splits each amplitude and stores Ah/Al straight
+// into the block's canonical no-swizzle K-major operand layout - the map from
+// (row, register) to operand slot is GF(2)-linear, so it is a precomputed
+// slot table (SetSlots), and no separate transpose pass exists.  One thread
+// issues the 12 MMAs per 128 rows and commits them to an mbarrier; every
+// thread then reads its row of D back from tensor memory (tcgen05.ld
+// 32x32b.x64), which is the next block's source layout.  The blocks' B
+// operands (Bh, Bl: 16 KB per block) arrive once per CTA by bulk async
+// copies (cp.async.bulk) and stay in shared memory.
+//
+// Every wait is bounded; a wait that gives up sets g_tc_status, later CTAs
+// skip their work, and the CTA still frees its tensor memory.
+#include <algorithm>
+#include <cstdint>
+
+#include "qg_device.cuh"
+#include "qg_internal.h"
+#include "qg_regstage.cuh"
+
+namespace qg {
+
+__device__ unsigned g_tc_status;
+
+namespace {
+
+using rs::Swz;
+using rs::reg_slot;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start address, leading-dimension byte
+// offset (between core matrices along K), stride-dimension byte offset
+// (between 8-row groups), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
+           ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D = F32, A = B = F16, both K-major,
+// N = 64, M = 128.
+constexpr unsigned kIdescF16 = (1u << 4) | (0u << 7) | (0u << 10) | ((64u >> 3) << 17) |
+                               ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(unsigned dtmem, uint64_t a, uint64_t b, unsigned acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %3, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n\t}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(acc), "r"(kIdescF16)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(unsigned bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+// Bounded wait for the completion of the phase with the given parity.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    for (int i = 0; i < (1 << 20); ++i) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_x64(unsigned taddr, unsigned (&u)[64]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n"
+        : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]),
+          "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]),
+          "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31]),
+          "=r"(u[32]), "=r"(u[33]), "=r"(u[34]), "=r"(u[35]), "=r"(u[36]), "=r"(u[37]), "=r"(u[38]), "=r"(u[39]),
+          "=r"(u[40]), "=r"(u[41]), "=r"(u[42]), "=r"(u[43]), "=r"(u[44]), "=r"(u[45]), "=r"(u[46]), "=r"(u[47]),
+          "=r"(u[48]), "=r"(u[49]), "=r"(u[50]), "=r"(u[51]), "=r"(u[52]), "=r"(u[53]), "=r"(u[54]), "=r"(u[55]),
+          "=r"(u[56]), "=r"(u[57]), "=r"(u[58]), "=r"(u[59]), "=r"(u[60]), "=r"(u[61]), "=r"(u[62]), "=r"(u[63])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+// (hi, lo) FP16 split of a complex amplitude (x, y): hi = f16x2(x, y)
+// rounded to nearest, lo = f16x2 of the residuals.
+__device__ __forceinline__ void split_f16x2(float x, float y, unsigned &hi, unsigned &lo) {
+    asm("{\n\t.reg .f32 hx, hy;\n\t.reg .b16 bx, by;\n\t"
+        "cvt.rn.f16x2.f32 %0, %3, %2;\n\t"
+        "mov.b32 {bx, by}, %0;\n\t"
+        "cvt.f32.f16 hx, bx;\n\t"
+        "cvt.f32.f16 hy, by;\n\t"
+        "sub.f32 hx, %2, hx;\n\t"
+        "sub.f32 hy, %3, hy;\n\t"
+        "cvt.rn.f16x2.f32 %1, hy, hx;\n\t}\n"
+        : "=r"(hi), "=r"(lo)
+        : "f"(x), "f"(y));
+}
+
+// The state is carried scaled by 2^12 through the blocks of a stage.
+constexpr float kScale = 4096.f, kUnscale = 1.f / 4096.f;
+
+}  // namespace
+
+__device__ __forceinline__ void group_sync(unsigned id, unsigned threads) {
+    asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(threads) : "memory");
+}
+
+// Persistent kernel, one CTA per SM.  The CTA holds every block operand of
+// the stage in shared memory (loaded once) and G independent tile groups of
+// 128 * RT threads (RT = 128-row groups per tile: tile lanes m = 12 for
+// RT = 1, 13 for RT = 2); each group walks its own tiles with its own
+// operand buffers, tensor-memory columns and mbarrier, so the groups overlap
+// one another's loads, splits and products on the SM's tensor core.
+template <int RT, int G>
+__global__ void __launch_bounds__(128 * RT * G, 1)
+k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long long tiles) {
+    constexpr int m = RT == 1 ? 12 : 13;
+    constexpr int t = m - 5;
+    constexpr unsigned TG = 128u * RT;                  // threads per group
+    constexpr unsigned T = TG * G;
+    constexpr unsigned kColsGroup = 64u * RT;
+    constexpr unsigned kCols = kColsGroup * G <= 32 ? 32 : (kColsGroup * G <= 64 ? 64 :
+                               (kColsGroup * G <= 128 ? 128 : (kColsGroup * G <= 256 ? 256 : 512)));
+    constexpr unsigned kBBytes = 2u * 64u * 64u * 2u;   // Bh, Bl of one block in FP16
+    constexpr unsigned kABytes = 4u << m;               // one FP16 operand of a tile
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    const int nb = d.nblocks;
+    unsigned char *Bs = smraw + (size_t)G * 2 * kABytes;
+    long long *sdep = (long long *)(Bs + (size_t)nb * kBBytes);
+    SetSlots *sset = (SetSlots *)(sdep + 32);
+    __shared__ __align__(8) unsigned long long bar_mma[G], bar_b;
+    __shared__ unsigned tmem_sh;
+    __shared__ int abort_sh[G];
+    const unsigned tid = threadIdx.x;
+    const unsigned warp = tid >> 5;
+    const unsigned g = tid / TG, lt = tid % TG;
+    unsigned *Ah = (unsigned *)(smraw + (size_t)g * 2 * kABytes);  // f16x2 per amplitude
+    unsigned *Al = Ah + (1 << m);
+    float2 *tile_sm = (float2 *)Ah;                     // natural tile (aliases Ah, Al)
+
+    if (tid == 0) abort_sh[0] = *(volatile unsigned *)&g_tc_status != 0u;
+    __syncthreads();
+    if (abort_sh[0]) return;
+    __syncthreads();
+
+    const unsigned bb = smem_u32(&bar_b), bmma = smem_u32(&bar_mma[g]);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_u32(&tmem_sh)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid < G) {
+        mbar_init(smem_u32(&bar_mma[tid]), 1);
+        abort_sh[tid] = 0;
+    }
+    if (tid == 0) {
+        mbar_init(bb, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (tid < 32) sdep[tid] = d.dep_hi[tid];
+    rs::copy_sets(sset, d.sets, nb + 1, tid, T);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = tmem_sh + g * kColsGroup + 64u * ((warp >> 2) % RT) +
+                          ((32u * (warp & 3u)) << 16);    // this warp's lanes and columns
+    const unsigned dcol0 = tmem_sh + g * kColsGroup;       // the group's accumulator
+    if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bb),
+                     "r"((unsigned)nb * kBBytes)
+                     : "memory");
+        for (int b = 0; b < nb; ++b)
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+                "[%3];\n" ::"r"(smem_u32(Bs + (size_t)b * kBBytes)),
+                "l"(d.bmats + (size_t)b * (kBBytes / 2)), "r"(kBBytes), "r"(bb)
+                : "memory");
+    }
+
+    // Load layout: thread r = tile lanes 0..t-1, register j = tile lanes t..m-1.
+    const int lr = d.lowrun < t ? d.lowrun : t;
+    idx_t dt = (idx_t)(lt & ((1u << lr) - 1u));
+    for (int b = lr; b < t; ++b)
+        if (lt & (1u << b)) dt |= 1LL << d.hi_pos[b - d.lowrun];
+    const unsigned pt = Swz<float>::f(lt);
+    const unsigned gbar = 1u + g;                          // the group's named barrier
+    unsigned phase = 0;
+    bool ok = true, b_ready = false;
+
+    for (long long tl = (long long)blockIdx.x * G + g; tl < tiles && ok;
+         tl += (long long)gridDim.x * G) {
+        float2 *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
+        float v[64];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            float2 x = gp[sdep[j]];
+            v[2 * j] = x.x * kScale;
+            v[2 * j + 1] = x.y * kScale;
+        }
+        for (int b = 0; b < nb; ++b) {
+            const SetSlots &ss = sset[b];
+            const unsigned base = (unsigned)ss.lo[lt & 31u] ^ (unsigned)ss.hi[lt >> 5];
+            unsigned q[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) q[k] = ss.q[k];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const unsigned slot = reg_slot<5>(base, q, j);
+                unsigned h, l;
+                split_f16x2(v[2 * j], v[2 * j + 1], h, l);
+                Ah[slot] = h;
+                Al[slot] = l;
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            group_sync(gbar, TG);
+            if (lt == 0) {
+                if (!b_ready) b_ready = mbar_wait(bb, 0u);
+                if (b_ready) {
+                    tc_fence_after();
+                    const unsigned ah = smem_u32(Ah), al = smem_u32(Al),
+                                   bh = smem_u32(Bs + (size_t)b * kBBytes), bl = bh + kBBytes / 2;
+#pragma unroll
+                    for (int mt = 0; mt < RT; ++mt) {
+#pragma unroll
+                        for (int ks = 0; ks < 4; ++ks) {
+                            const unsigned aoff = 16384u * mt + 4096u * ks, boff = 2048u * ks;
+                            const uint64_t dah = smem_desc(ah + aoff, 128, 256);
+                            const uint64_t dal = smem_desc(al + aoff, 128, 256);
+                            const uint64_t dbh = smem_desc(bh + boff, 1024, 128);
+                            const uint64_t dbl = smem_desc(bl + boff, 1024, 128);
+                            const unsigned dcol = dcol0 + 64u * mt;
+                            mma_f16(dcol, dah, dbh, ks > 0 ? 1u : 0u);
+                            mma_f16(dcol, dah, dbl, 1u);
+                            mma_f16(dcol, dal, dbh, 1u);
+                        }
+                    }
+                    mma_commit(bmma);
+                } else {
+                    atomicOr(&g_tc_status, 1u);
+                    abort_sh[g] = 1;
+                    mbar_arrive(bmma);
+                }
+            }
+            const bool got = mbar_wait(bmma, phase);
+            phase ^= 1u;
+            if (!got) {
+                abort_sh[g] = 1;
+                atomicOr(&g_tc_status, 2u);
+            }
+            // One decision for the whole group, so that its threads leave
+            // together.
+            group_sync(gbar, TG);
+            if (abort_sh[g]) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            unsigned u[64];
+            tmem_ld_x64(tmem, u);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(u[i]);
+        }
+        tc_fence_before();
+        group_sync(gbar, TG);  // every thread's products read: the buffers are free
+        if (!ok) break;
+        // Last layout -> swizzled natural tile -> load layout -> global.
+        {
+            const SetSlots &ss = sset[nb];
+            const unsigned base = (unsigned)ss.lo[lt & 31u] ^ (unsigned)ss.hi[lt >> 5];
+            unsigned q[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) q[k] = ss.q[k];
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                tile_sm[reg_slot<5>(base, q, j)] =
+                    make_float2(v[2 * j] * kUnscale, v[2 * j + 1] * kUnscale);
+        }
+        group_sync(gbar, TG);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) gp[sdep[j]] = tile_sm[pt ^ Swz<float>::f((unsigned)j << t)];
+        group_sync(gbar, TG);  // the natural tile is read before the next splits
+    }
+    // A group whose bulk-copy wait never ran still owns an outstanding copy
+    // only if it never issued an MMA; the CTA waits for it before exiting.
+    if (tid == 0 && !b_ready) mbar_wait(bb, 0u);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_sh),
+                     "r"(kCols)
+                     : "memory");
+    }
+}
+
+// Shared memory of the persistent kernel: G tiles' operand pairs, the
+// stage's block operands, the offset table and the slot tables.
+static size_t tstage_smem(int m, int groups, int nblocks) {
+    return (size_t)groups * 2 * ((size_t)4 << m) + (size_t)nblocks * 2 * 64 * 64 * 2 +
+           32 * sizeof(long long) + sizeof(SetSlots) * (size_t)(nblocks + 1);
+}
+
+int tstage_max_blocks(int m) {
+    const int groups = m == 12 ? 4 : 2;
+    int nb = 1;
+    while (nb < kMaxTcBlocks && tstage_smem(m, groups, nb + 1) + 2048 <= 227 * 1024) ++nb;
+    return nb;
+}
+
+void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream) {
+    if (d.m != 12 && d.m != 13) fail(2, "tensor stage: tile lanes must be 12 or 13 (got %d)", d.m);
+    if (d.nblocks < 1 || d.nblocks > tstage_max_blocks(d.m))
+        fail(2, "tensor stage: bad block count %d", d.nblocks);
+    if (((uintptr_t)d.bmats & 15u) != 0) fail(2, "tensor stage: operand array misaligned");
+    const long long tiles = 1LL << (d.n - d.m);
+    int dev = 0, sms = 0;
+    QG_CUDA(cudaGetDevice(&dev));
+    QG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    auto launch = [&](auto kern, int groups, int threads) {
+        const size_t smem = tstage_smem(d.m, groups, d.nblocks);
+        QG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const long long ctas = std::min<long long>((tiles + groups - 1) / groups, sms);
+        kern<<<(unsigned)ctas, threads, smem, stream>>>((float2 *)state, d, tiles);
+    };
+    if (d.m == 12)
+        launch(k_tstage<1, 4>, 4, 512);
+    else
+        launch(k_tstage<2, 2>, 2, 512);
+    QG_CUDA(cudaGetLastError());
+}
+
+int tstage_status(bool reset) {
+    unsigned v = 0;
+    QG_CUDA(cudaMemcpyFromSymbol(&v, g_tc_status, sizeof(v)));
+    if (reset && v) {
+        unsigned z = 0;
+        QG_CUDA(cudaMemcpyToSymbol(g_tc_status, &z, sizeof(z)));
+    }
+    return (int)v;
+}
+
+}  // namespace qg

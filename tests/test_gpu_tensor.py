@@ -1,0 +1,116 @@
+"""GPU parity of the tensor-core stage kernel (k_tstage): complex64 stages of
+12- and 13-lane tiles run as fused 5-lane blocks, each a 32x32 complex
+matrix applied by tcgen05 products in 3xTF32.
+
+Against the oracle's complex128 run: max amplitude error < 1e-5 and
+fidelity error |1 - <psi64|psi32>| < 1e-5 (the complex64 bound of the
+CUDA-core stage kernel's tests); every bounded wait inside the kernel must
+have completed (status word 0), and the tensor kernel must actually have
+run (its launch counter)."""
+import numpy as np
+import pytest
+
+from oracle import statevec as sv
+from tests.gpu_helpers import new_state, apply_ops, random_ops, fidelity_error
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def tensor_mode():
+    from qgate_gb300 import _native as nat
+    nat.tensor_stage_status(reset=True)
+    nat.timing_enable(True)
+    nat.timing_read('', reset=True)
+    nat.set_tensor_blocks(True)
+    yield nat
+    nat.set_tensor_blocks(False)
+    nat.set_fusion(0)
+    nat.timing_enable(False)
+
+
+def _u3_cx(rng, n, depth):
+    ops = []
+    for _ in range(depth):
+        ang = rng.uniform(0, 2 * np.pi, (n, 3))
+        ops += [('g', 'U', tuple(ang[q]), False, q, ()) for q in range(n)]
+        perm = rng.permutation(n)
+        ops += [('g', 'X', (), False, int(perm[2 * k + 1]), (int(perm[2 * k]),))
+                for k in range(n // 2)]
+    return ops
+
+
+def _run(rt, n, ops):
+    qs = new_state(rt, n, np.float32)
+    apply_ops(qs, ops)
+    got = qs.get_raw()
+    qs.delete()
+    return got
+
+
+def _check(got, want):
+    err = np.max(np.abs(got.astype(np.complex128) - want))
+    ferr = fidelity_error(want, got)
+    assert err < 1e-5 and ferr < 1e-5, (err, ferr)
+
+
+@pytest.mark.parametrize('tile', [12, 13])
+@pytest.mark.parametrize('n', [13, 16])
+def test_tensor_stage_random_circuits(rt, tensor_mode, tile, n):
+    nat = tensor_mode
+    nat.set_fusion_params(nat.PREC_FP32, tile, 5, 0)
+    rng = np.random.default_rng(100 + 10 * tile + n)
+    circuits = [_u3_cx(rng, n, 3), random_ops(rng, n, 120, max_controls=2)]
+    for ops in circuits:
+        _check(_run(rt, n, ops), sv.run_ops(n, ops, np.complex128))
+    launches, _ = nat.timing_read('tstage')
+    assert launches > 0
+    assert nat.tensor_stage_status() == 0
+
+
+def test_tensor_stage_tile_equals_state(rt, tensor_mode):
+    """n = tile lanes: one tile covers the whole state (grid of one CTA)."""
+    nat = tensor_mode
+    nat.set_fusion_params(nat.PREC_FP32, 12, 5, 0)
+    rng = np.random.default_rng(12)
+    ops = _u3_cx(rng, 12, 4)
+    _check(_run(rt, 12, ops), sv.run_ops(12, ops, np.complex128))
+    assert nat.timing_read('tstage')[0] > 0
+    assert nat.tensor_stage_status() == 0
+
+
+def test_tensor_stage_many_blocks_and_small_blocks(rt, tensor_mode):
+    """Three-lane gates on random triples give stages of more blocks than one
+    launch holds (split over launches) and blocks of fewer than 5 lanes
+    (padded with identity lanes); single-lane diagonal runs give blocks of
+    one lane."""
+    nat = tensor_mode
+    nat.set_fusion_params(nat.PREC_FP32, 13, 5, 0)
+    rng = np.random.default_rng(3)
+    n = 15
+    ops = []
+    for _ in range(90):
+        a, b, c = rng.permutation(n)[:3]
+        ops.append(('g', 'U', tuple(rng.uniform(0, 2 * np.pi, 3)), False, int(a),
+                    (int(b), int(c))))
+    ops += [('g', 'T', (), False, q, ()) for q in range(n)]
+    ops += [('g', 'RZ', (0.3,), False, 14, ())]
+    _check(_run(rt, n, ops), sv.run_ops(n, ops, np.complex128))
+    assert nat.tensor_stage_status() == 0
+
+
+def test_tensor_stage_matches_cuda_core_stage(rt, tensor_mode):
+    """Same 20-qubit circuit (the 30-qubit benchmark's structure), tensor
+    blocks vs the register-resident CUDA-core stage kernel vs the oracle."""
+    nat = tensor_mode
+    rng = np.random.default_rng(20)
+    n = 20
+    ops = _u3_cx(rng, n, 4)
+    want = sv.run_ops(n, ops, np.complex128)
+    nat.set_fusion_params(nat.PREC_FP32, 13, 5, 0)
+    got_tc = _run(rt, n, ops)
+    nat.set_tensor_blocks(False)
+    got_cc = _run(rt, n, ops)
+    _check(got_tc, want)
+    _check(got_cc, want)
+    assert nat.tensor_stage_status() == 0
