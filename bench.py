@@ -128,11 +128,11 @@ def measured_peak_hbm():
         return 6800.0, 'fallback'
 
 
-def stage_traffic_per_launch(n, cs):
+def stage_traffic_per_launch(n, cs, kernel_class='stage'):
     """DRAM bytes per fused-stage launch: bytes per amplitude from the ncu
     capture recorded in profiles/stage_traffic.txt (a smaller state, same
     kernel; traffic grows in proportion to the amplitudes), scaled to 2^n."""
-    key = 'c64' if cs == 8 else 'c128'
+    key = ('c64' if cs == 8 else 'c128') + ('_tensor' if kernel_class == 'tstage' else '')
     try:
         with open(os.path.join(ROOT, 'profiles', 'stage_traffic.txt')) as f:
             for line in f:
@@ -287,14 +287,15 @@ def run_gb300(args):
     dom = max(timing.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_launches, dom_ms) = dom
     peak, peak_kind = measured_peak_hbm()
-    if dom_name == 'stage':
+    if dom_name in ('stage', 'tstage'):
         alg = 2 * (1 << n) * cs
-        traffic = stage_traffic_per_launch(n, cs)
+        traffic = stage_traffic_per_launch(n, cs, dom_name)
     else:
         alg = stats['bytes'] / max(1, stats['passes'])
         traffic = None
     achieved = alg / (dom_ms / dom_launches / 1e3) / 1e9 if dom_launches else 0.
     roofline = {'kernel': {'stage': 'k_rstage (fused register-resident stage)',
+                           'tstage': 'k_tstage (fused 5-lane blocks on tcgen05 tensor cores)',
                            'gate': 'k_pairs (single gate)'}.get(dom_name, dom_name),
                 'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                 'frac': achieved / peak, 'peak_source': peak_kind,
@@ -340,7 +341,8 @@ def run_gb300(args):
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': args.dtype, 'data': 'synthetic',
             'config': config_block(args, {
-                'fusion': {k: tuned.get(k) for k in ('tile_lanes', 'reg_lanes', 'cost_budget')},
+                'fusion': {k: tuned.get(k) for k in ('tile_lanes', 'reg_lanes', 'cost_budget',
+                                                    'tensor', 'prefetch')},
                 'value_definition': 'unfused gate-pass bytes (each gate as its own read+write '
                                     'sweep of the amplitudes it touches) per second',
                 'hbm_gbs_actual': hbm_actual,

@@ -136,8 +136,9 @@ int qg_qubit_processor_calc_pauli_expectation(qg_handle proc, qg_handle qstates,
 int qg_qubit_processor_calc_norm(qg_handle proc, qg_handle qstates, double *out);
 
 /* Extension: gate fusion control.  max_tile_lanes = lanes staged per tile in
- * shared memory by the fused stage kernel (0 = autotuned default, 1 = off:
- * every gate is its own pass).  Pending gates are flushed at every
+ * shared memory by the fused stage kernel (0 = the defaults: 12-lane tiles,
+ * 4 register lanes, no cost budget, tensor-core blocks on, pipelining off;
+ * 1 = off: every gate is its own pass).  Pending gates are flushed at every
  * observation, join, measure or synchronize. */
 int qg_set_fusion(int max_tile_lanes);
 /* Extension: fusion parameters for one precision: lanes per shared-memory
@@ -146,11 +147,13 @@ int qg_set_fusion(int max_tile_lanes);
  * per-amplitude instruction budget that closes a stage early (0 = none). */
 int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budget);
 /* Extension: 1 runs large fused stages with the persistent, double-buffered
- * stage kernel; 0 (default) with one CTA per tile, which keeps more warps
- * resident per SM. */
+ * stage kernel (and 12-lane tensor-core stages with the variant that
+ * prefetches each group's next tile into registers); 0 (default) with one
+ * CTA per tile (tensor-core stages: four groups per SM), which keeps more
+ * warps resident per SM. */
 int qg_set_stage_pipelining(int on);
-/* Extension: 1 runs complex64 stages of 12- or 13-lane tiles as fused 5-lane
- * blocks (32x32 complex matrices) on the tensor cores, 0 (default) on the
+/* Extension: 1 (default) runs complex64 stages of 12- or 13-lane tiles as
+ * fused 5-lane blocks (32x32 complex matrices) on the tensor cores, 0 on the
  * register-resident CUDA-core stage kernel.  No reference counterpart: the
  * reference applies one gate per pass
  * (qgate/simulator/src/CUDAQubitProcessor.cpp:271, applyGate). */

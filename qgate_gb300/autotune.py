@@ -1,12 +1,14 @@
-"""Autotuner for the fused-stage kernel's tile shape.
+"""Autotuner for the fused-stage kernels' tile shape.
 
 The fusion planner packs gates into shared-memory tiles of `tile_lanes`
 lanes, run by the register-resident stage kernel with `reg_lanes` lanes per
 thread's registers, and closes a stage when its estimated per-amplitude
-instruction count passes `cost_budget`.  Which shape is fastest depends on
-the state size, the precision and the gate mix, so this module times a
-candidate grid on a caller-supplied circuit and keeps the best shape per
-(device, lanes, precision) in a JSON cache next to the package.
+instruction count passes `cost_budget`; complex64 stages of 12 or 13 lanes
+can instead run on the tensor cores as fused 5-lane blocks (`tensor`), with
+or without the next-tile prefetch (`prefetch`).  Which shape is fastest
+depends on the state size, the precision and the gate mix, so this module
+times a candidate grid on a caller-supplied circuit and keeps the best
+shape per (device, lanes, precision) in a JSON cache next to the package.
 
     from qgate_gb300 import autotune
     best = autotune.tune(n_lanes, np.float32, ops)   # ops: [(name, args, target, controls)]
@@ -23,18 +25,26 @@ from .circuit import gate_type
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), '_tuning.json')
 
-# (tile_lanes, reg_lanes, cost_budget)
+# (tile_lanes, reg_lanes, cost_budget, tensor, prefetch)
 CANDIDATES = {
-    np.float32: [(10, 4, 0), (11, 4, 0), (11, 5, 0), (12, 4, 0), (12, 5, 0), (13, 4, 0),
-                 (13, 5, 0), (12, 4, 130), (11, 4, 130)],
-    np.float64: [(10, 4, 0), (11, 4, 0), (12, 4, 0), (13, 4, 0), (11, 3, 0)],
+    np.float32: [(10, 4, 0, 0, 0), (11, 4, 0, 0, 0), (11, 5, 0, 0, 0), (12, 4, 0, 0, 0),
+                 (12, 5, 0, 0, 0), (13, 4, 0, 0, 0), (13, 5, 0, 0, 0), (12, 4, 130, 0, 0),
+                 (11, 4, 130, 0, 0), (12, 5, 0, 1, 0), (12, 5, 0, 1, 1), (13, 5, 0, 1, 0)],
+    np.float64: [(10, 4, 0, 0, 0), (11, 4, 0, 0, 0), (12, 4, 0, 0, 0), (13, 4, 0, 0, 0),
+                 (11, 3, 0, 0, 0)],
 }
+_VERSION = 'v2'
+
+
+def _norm(c):
+    c = tuple(c)
+    return c + (0,) * (5 - len(c))
 
 
 def _key(n_lanes, dtype):
     info = nat.device_info()
-    return '%d.%d/%d/%s' % (info['cc_major'], info['cc_minor'], n_lanes,
-                            'c128' if dtype == np.float64 else 'c64')
+    return '%s/%d.%d/%d/%s' % (_VERSION, info['cc_major'], info['cc_minor'], n_lanes,
+                               'c128' if dtype == np.float64 else 'c64')
 
 
 def _load():
@@ -52,6 +62,8 @@ def _prec(dtype):
 def apply(best):
     nat.set_fusion_params(best['prec'], best['tile_lanes'], best['reg_lanes'],
                           best['cost_budget'])
+    nat.set_tensor_blocks(best.get('tensor', 0))
+    nat.call('qg_set_stage_pipelining', int(best.get('prefetch', 0)))
 
 
 def tune(n_lanes, dtype, ops, repeats=2, use_cache=True, candidates=None):
@@ -78,22 +90,27 @@ def tune(n_lanes, dtype, ops, repeats=2, use_cache=True, candidates=None):
 
     prec = _prec(dtype)
     results = []
-    for tile, rl, budget in (candidates or CANDIDATES[dtype]):
-        if tile > n_lanes:
+    for cand in (candidates or CANDIDATES[dtype]):
+        tile, rl, budget, tensor, prefetch = _norm(cand)
+        if tile > n_lanes or (tensor and dtype == np.float64):
             continue
         nat.set_fusion_params(prec, tile, rl, budget)
+        nat.set_tensor_blocks(tensor)
+        nat.call('qg_set_stage_pipelining', prefetch)
         run()
         t0 = time.perf_counter()
         for _ in range(repeats):
             run()
         dt = (time.perf_counter() - t0) / repeats
-        results.append((dt, tile, rl, budget))
+        results.append((dt, tile, rl, budget, tensor, prefetch))
     qs.delete()
+    nat.set_tensor_blocks(0)
+    nat.call('qg_set_stage_pipelining', 0)
     results.sort()
-    dt, tile, rl, budget = results[0]
+    dt, tile, rl, budget, tensor, prefetch = results[0]
     best = {'prec': prec, 'tile_lanes': tile, 'reg_lanes': rl, 'cost_budget': budget,
-            'circuit_ms': dt * 1e3,
-            'table': [[r[1], r[2], r[3], r[0] * 1e3] for r in results]}
+            'tensor': tensor, 'prefetch': prefetch, 'circuit_ms': dt * 1e3,
+            'table': [list(r[1:]) + [r[0] * 1e3] for r in results]}
     cache[key] = best
     try:
         with open(CACHE, 'w') as f:

@@ -150,13 +150,13 @@ struct Device {
     // Fusion parameters, indexed by prec ([1] fp64, [2] fp32): lanes per
     // shared-memory tile, lanes per thread's registers, per-amplitude cost
     // budget of a stage (0 = unlimited).
-    int tile_lanes[3] = {0, 12, 13};
+    int tile_lanes[3] = {0, 12, 12};
     int reg_lanes[3] = {0, 4, 4};
     int cost_budget[3] = {0, 0, 0};
     bool pipelined = false;  // persistent double-buffered stage kernel (opt-in)
     // complex64 stages on 12- or 13-lane tiles as fused 5-lane blocks on the
-    // tensor cores (opt-in; the autotuner may select it).
-    bool tensor_blocks = false;
+    // tensor cores (default; 0 selects the register-resident CUDA-core stage).
+    bool tensor_blocks = true;
     // Ring of split block operands: pinned host staging and its device copy.
     static constexpr size_t kBRingBytes = 32ull << 20;
     unsigned short *h_bring = nullptr, *d_bring = nullptr;
@@ -744,7 +744,7 @@ static void run_tstage(Device &d, States *s, const TileLanes &tl,
         desc.sets[nb] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
         QG_CUDA(cudaMemcpyAsync(db, hb, bytes, cudaMemcpyHostToDevice, d.stream));
         d.bring_off += bytes;
-        timed(d, "tstage", [&] { launch_tstage(s->d, desc, d.stream); });
+        timed(d, "tstage", [&] { launch_tstage(s->d, desc, d.stream, d.pipelined); });
         d.n_passes += 1;
         d.n_bytes += 2 * ((long long)1 << n) * (long long)complex_size(s->prec);
     }
@@ -1470,12 +1470,14 @@ int qg_set_fusion(int max_tile_lanes) {
         fail(QG_ERR_VALUE, "max_tile_lanes must be in [0, %d].", kMaxTileLanes);
     flush_all();
     if (max_tile_lanes == 0) {
-        g_dev.tile_lanes[kFP32] = 13;
+        g_dev.tile_lanes[kFP32] = 12;
         g_dev.tile_lanes[kFP64] = 12;
         g_dev.reg_lanes[kFP32] = 4;
         g_dev.reg_lanes[kFP64] = 4;
         g_dev.cost_budget[kFP32] = 0;
         g_dev.cost_budget[kFP64] = 0;
+        g_dev.tensor_blocks = true;
+        g_dev.pipelined = false;
     } else {
         g_dev.tile_lanes[kFP32] = max_tile_lanes;
         g_dev.tile_lanes[kFP64] = std::min(max_tile_lanes, 13);

@@ -155,7 +155,9 @@ struct TcStageDesc {
     const unsigned short *bmats;
     SetSlots sets[kMaxTcBlocks + 1];
 };
-void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream);
+// prefetch: the 12-lane variant whose groups load their next tile while
+// running the current one.
+void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool prefetch);
 // Blocks one tensor-stage launch holds (its operands stay in shared memory).
 int tstage_max_blocks(int m);
 // Status word of the tensor stage kernels (nonzero: a bounded wait gave up).

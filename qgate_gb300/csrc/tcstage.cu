@@ -156,7 +156,10 @@ __device__ __forceinline__ void group_sync(unsigned id, unsigned threads) {
 // RT = 1, 13 for RT = 2); each group walks its own tiles with its own
 // operand buffers, tensor-memory columns and mbarrier, so the groups overlap
 // one another's loads, splits and products on the SM's tensor core.
-template <int RT, int G>
+//
+// PF: each group loads its next tile into registers while it runs the
+// blocks of the current one (64 more registers per thread, so fewer groups).
+template <int RT, int G, bool PF>
 __global__ void __launch_bounds__(128 * RT * G, 1)
 k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long long tiles) {
     constexpr int m = RT == 1 ? 12 : 13;
@@ -171,8 +174,7 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
     extern __shared__ __align__(1024) unsigned char smraw[];
     const int nb = d.nblocks;
     unsigned char *Bs = smraw + (size_t)G * 2 * kABytes;
-    long long *sdep = (long long *)(Bs + (size_t)nb * kBBytes);
-    SetSlots *sset = (SetSlots *)(sdep + 32);
+    SetSlots *sset = (SetSlots *)(Bs + (size_t)nb * kBBytes);
     __shared__ __align__(8) unsigned long long bar_mma[G], bar_b;
     __shared__ unsigned tmem_sh;
     __shared__ int abort_sh[G];
@@ -204,7 +206,6 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
         mbar_init(bb, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    if (tid < 32) sdep[tid] = d.dep_hi[tid];
     rs::copy_sets(sset, d.sets, nb + 1, tid, T);
     tc_fence_before();
     __syncthreads();
@@ -230,19 +231,64 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
     for (int b = lr; b < t; ++b)
         if (lt & (1u << b)) dt |= 1LL << d.hi_pos[b - d.lowrun];
     const unsigned pt = Swz<float>::f(lt);
+    // Global offset of register j: XOR of e[k] over the set bits k of j.
+    long long e[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) e[k] = d.dep_hi[1 << k];
+    auto roff = [&](int j) {
+        long long o = 0;
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+            if (j >> k & 1) o ^= e[k];
+        return o;
+    };
     const unsigned gbar = 1u + g;                          // the group's named barrier
     unsigned phase = 0;
     bool ok = true, b_ready = false;
 
-    for (long long tl = (long long)blockIdx.x * G + g; tl < tiles && ok;
-         tl += (long long)gridDim.x * G) {
-        float2 *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
-        float v[64];
+    const long long tstep = (long long)gridDim.x * G;
+    float2 w[PF ? 32 : 1];
+    if (PF) {
+        const long long tl0 = (long long)blockIdx.x * G + g;
+        if (tl0 < tiles) {
+            const float2 *gp0 = s + (insert_zeros((idx_t)tl0, d.ins_pos, d.nins) | dt);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            float2 x = gp[sdep[j]];
-            v[2 * j] = x.x * kScale;
-            v[2 * j + 1] = x.y * kScale;
+            for (int j = 0; j < (PF ? 32 : 1); ++j) w[j] = gp0[roff(j)];
+        }
+    }
+    // Without PF the next tile's loads are issued into v once the finished
+    // tile has been staged in shared memory, before it is copied out, so
+    // they are in flight during the copy-out; the scale is applied after.
+    unsigned v[64];  // floats (bits): row lt of the current layout
+    if (!PF) {
+        const long long tl0 = (long long)blockIdx.x * G + g;
+        if (tl0 < tiles) {
+            const float2 *gp0 = s + (insert_zeros((idx_t)tl0, d.ins_pos, d.nins) | dt);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float2 x = gp0[roff(j)];
+                v[2 * j] = __float_as_uint(x.x);
+                v[2 * j + 1] = __float_as_uint(x.y);
+            }
+        }
+    }
+    for (long long tl = (long long)blockIdx.x * G + g; tl < tiles && ok; tl += tstep) {
+        float2 *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
+        if (PF) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                v[2 * j] = __float_as_uint(w[PF ? j : 0].x * kScale);
+                v[2 * j + 1] = __float_as_uint(w[PF ? j : 0].y * kScale);
+            }
+            if (tl + tstep < tiles) {
+                const float2 *gn =
+                    s + (insert_zeros((idx_t)(tl + tstep), d.ins_pos, d.nins) | dt);
+#pragma unroll
+                for (int j = 0; j < (PF ? 32 : 1); ++j) w[j] = gn[roff(j)];
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 64; ++i) v[i] = __float_as_uint(__uint_as_float(v[i]) * kScale);
         }
         for (int b = 0; b < nb; ++b) {
             const SetSlots &ss = sset[b];
@@ -254,7 +300,7 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
             for (int j = 0; j < 32; ++j) {
                 const unsigned slot = reg_slot<5>(base, q, j);
                 unsigned h, l;
-                split_f16x2(v[2 * j], v[2 * j + 1], h, l);
+                split_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]), h, l);
                 Ah[slot] = h;
                 Al[slot] = l;
             }
@@ -302,11 +348,8 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
                 break;
             }
             tc_fence_after();
-            unsigned u[64];
-            tmem_ld_x64(tmem, u);
+            tmem_ld_x64(tmem, v);
             tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(u[i]);
         }
         tc_fence_before();
         group_sync(gbar, TG);  // every thread's products read: the buffers are free
@@ -321,11 +364,21 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
 #pragma unroll
             for (int j = 0; j < 32; ++j)
                 tile_sm[reg_slot<5>(base, q, j)] =
-                    make_float2(v[2 * j] * kUnscale, v[2 * j + 1] * kUnscale);
+                    make_float2(__uint_as_float(v[2 * j]) * kUnscale,
+                                __uint_as_float(v[2 * j + 1]) * kUnscale);
         }
         group_sync(gbar, TG);
+        if (!PF && tl + tstep < tiles) {
+            const float2 *gn = s + (insert_zeros((idx_t)(tl + tstep), d.ins_pos, d.nins) | dt);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) gp[sdep[j]] = tile_sm[pt ^ Swz<float>::f((unsigned)j << t)];
+            for (int j = 0; j < 32; ++j) {
+                const float2 x = gn[roff(j)];
+                v[2 * j] = __float_as_uint(x.x);
+                v[2 * j + 1] = __float_as_uint(x.y);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) gp[roff(j)] = tile_sm[pt ^ Swz<float>::f((unsigned)j << t)];
         group_sync(gbar, TG);  // the natural tile is read before the next splits
     }
     // A group whose bulk-copy wait never ran still owns an outstanding copy
@@ -342,20 +395,24 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
 }
 
 // Shared memory of the persistent kernel: G tiles' operand pairs, the
-// stage's block operands, the offset table and the slot tables.
+// stage's block operands and the slot tables.
 static size_t tstage_smem(int m, int groups, int nblocks) {
     return (size_t)groups * 2 * ((size_t)4 << m) + (size_t)nblocks * 2 * 64 * 64 * 2 +
-           32 * sizeof(long long) + sizeof(SetSlots) * (size_t)(nblocks + 1);
+           sizeof(SetSlots) * (size_t)(nblocks + 1);
 }
 
+// Groups per CTA: 12-lane tiles 4 groups of 128 threads (3 with the
+// next-tile prefetch), 13-lane tiles 2 groups of 256 threads.
+static int tstage_groups(int m, bool prefetch) { return m == 12 ? (prefetch ? 3 : 4) : 2; }
+
 int tstage_max_blocks(int m) {
-    const int groups = m == 12 ? 4 : 2;
+    const int groups = tstage_groups(m, false);
     int nb = 1;
     while (nb < kMaxTcBlocks && tstage_smem(m, groups, nb + 1) + 2048 <= 227 * 1024) ++nb;
     return nb;
 }
 
-void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream) {
+void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool prefetch) {
     if (d.m != 12 && d.m != 13) fail(2, "tensor stage: tile lanes must be 12 or 13 (got %d)", d.m);
     if (d.nblocks < 1 || d.nblocks > tstage_max_blocks(d.m))
         fail(2, "tensor stage: bad block count %d", d.nblocks);
@@ -370,10 +427,12 @@ void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream) {
         const long long ctas = std::min<long long>((tiles + groups - 1) / groups, sms);
         kern<<<(unsigned)ctas, threads, smem, stream>>>((float2 *)state, d, tiles);
     };
-    if (d.m == 12)
-        launch(k_tstage<1, 4>, 4, 512);
+    if (d.m == 12 && prefetch)
+        launch(k_tstage<1, 3, true>, 3, 384);
+    else if (d.m == 12)
+        launch(k_tstage<1, 4, false>, 4, 512);
     else
-        launch(k_tstage<2, 2>, 2, 512);
+        launch(k_tstage<2, 2, false>, 2, 512);
     QG_CUDA(cudaGetLastError());
 }
 

@@ -114,6 +114,7 @@ def test_register_stage_shapes(rt, dtype):
     wants = [sv.run_ops(n, ops, np.complex128) for ops in circuits]
     rls = (3, 4) if dtype == np.float64 else (3, 4, 5)
     tol = 1e-11 if dtype == np.float64 else 1e-5
+    nat.set_tensor_blocks(False)  # this test covers the CUDA-core stage kernel
     try:
         for tile in (6, 8, 9, 10, 11, 12, 13):
             for rl in rls:
@@ -143,6 +144,7 @@ def test_pipelined_stage_kernel_22q(rt, dtype):
     want = sv.run_ops(n, ops, np.complex128)
     tol = 1e-11 if dtype == np.float64 else 1e-5
     shapes = [(11, 4), (12, 4), (13, 4)] + ([(12, 5), (13, 5)] if dtype == np.float32 else [])
+    nat.set_tensor_blocks(False)  # this test covers the CUDA-core stage kernel
     try:
         for tile, rl in shapes:
             nat.set_fusion_params(prec, tile, rl, 0)

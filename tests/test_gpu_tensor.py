@@ -24,8 +24,7 @@ def tensor_mode():
     nat.timing_read('', reset=True)
     nat.set_tensor_blocks(True)
     yield nat
-    nat.set_tensor_blocks(False)
-    nat.set_fusion(0)
+    nat.set_fusion(0)  # the defaults (tensor blocks on)
     nat.timing_enable(False)
 
 
@@ -111,6 +110,26 @@ def test_tensor_stage_matches_cuda_core_stage(rt, tensor_mode):
     got_tc = _run(rt, n, ops)
     nat.set_tensor_blocks(False)
     got_cc = _run(rt, n, ops)
+    nat.set_tensor_blocks(True)
     _check(got_tc, want)
     _check(got_cc, want)
+    assert nat.tensor_stage_status() == 0
+
+
+def test_tensor_stage_prefetch_variant(rt, tensor_mode):
+    """The 12-lane variant whose groups prefetch their next tile into
+    registers (selected with stage pipelining on) against the oracle and
+    against the default variant (same arithmetic: identical results)."""
+    nat = tensor_mode
+    nat.set_fusion_params(nat.PREC_FP32, 12, 5, 0)
+    rng = np.random.default_rng(18)
+    n = 18
+    ops = _u3_cx(rng, n, 3) + random_ops(rng, n, 60, max_controls=2)
+    got = {}
+    for pf in (1, 0):
+        nat.call('qg_set_stage_pipelining', pf)
+        got[pf] = _run(rt, n, ops)
+    nat.call('qg_set_stage_pipelining', 0)
+    _check(got[1], sv.run_ops(n, ops, np.complex128))
+    assert np.array_equal(got[0], got[1])
     assert nat.tensor_stage_status() == 0
