@@ -141,6 +141,24 @@ __device__ __forceinline__ void split_f16x2(float x, float y, unsigned &hi, unsi
         : "f"(x), "f"(y));
 }
 
+// Visits the 32 registers of a thread in Gray-code order: f(j, p) with p =
+// base + offset of register j, where register j's offset is the sum of e[k]
+// over the set bits k of j.
+template <class P, class F>
+__device__ __forceinline__ void gray_walk(P *base, const long long (&e)[5], F f) {
+    P *p = base;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        const int j = i ^ (i >> 1);
+        if (i > 0) {
+            // gray(i) and gray(i - 1) differ in bit ctz(i)
+            const int k = (i & 1) ? 0 : (i & 2) ? 1 : (i & 4) ? 2 : (i & 8) ? 3 : 4;
+            p = (j >> k & 1) ? p + e[k] : p - e[k];
+        }
+        f(j, p);
+    }
+}
+
 // The state is carried scaled by 2^12 through the blocks of a stage.
 constexpr float kScale = 4096.f, kUnscale = 1.f / 4096.f;
 
@@ -231,17 +249,12 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
     for (int b = lr; b < t; ++b)
         if (lt & (1u << b)) dt |= 1LL << d.hi_pos[b - d.lowrun];
     const unsigned pt = Swz<float>::f(lt);
-    // Global offset of register j: XOR of e[k] over the set bits k of j.
+    // Global offset of register j: the sum (the bits are disjoint) of e[k]
+    // over the set bits k of j.  The loops below visit j in Gray-code order,
+    // so each step adds or subtracts one e[k] from a running pointer.
     long long e[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) e[k] = d.dep_hi[1 << k];
-    auto roff = [&](int j) {
-        long long o = 0;
-#pragma unroll
-        for (int k = 0; k < 5; ++k)
-            if (j >> k & 1) o ^= e[k];
-        return o;
-    };
     const unsigned gbar = 1u + g;                          // the group's named barrier
     unsigned phase = 0;
     bool ok = true, b_ready = false;
@@ -252,8 +265,7 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
         const long long tl0 = (long long)blockIdx.x * G + g;
         if (tl0 < tiles) {
             const float2 *gp0 = s + (insert_zeros((idx_t)tl0, d.ins_pos, d.nins) | dt);
-#pragma unroll
-            for (int j = 0; j < (PF ? 32 : 1); ++j) w[j] = gp0[roff(j)];
+            gray_walk(gp0, e, [&](int j, const float2 *p) { w[PF ? j : 0] = *p; });
         }
     }
     // Without PF the next tile's loads are issued into v once the finished
@@ -264,12 +276,11 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
         const long long tl0 = (long long)blockIdx.x * G + g;
         if (tl0 < tiles) {
             const float2 *gp0 = s + (insert_zeros((idx_t)tl0, d.ins_pos, d.nins) | dt);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const float2 x = gp0[roff(j)];
+            gray_walk(gp0, e, [&](int j, const float2 *p) {
+                const float2 x = *p;
                 v[2 * j] = __float_as_uint(x.x);
                 v[2 * j + 1] = __float_as_uint(x.y);
-            }
+            });
         }
     }
     for (long long tl = (long long)blockIdx.x * G + g; tl < tiles && ok; tl += tstep) {
@@ -283,8 +294,7 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
             if (tl + tstep < tiles) {
                 const float2 *gn =
                     s + (insert_zeros((idx_t)(tl + tstep), d.ins_pos, d.nins) | dt);
-#pragma unroll
-                for (int j = 0; j < (PF ? 32 : 1); ++j) w[j] = gn[roff(j)];
+                gray_walk(gn, e, [&](int j, const float2 *p) { w[PF ? j : 0] = *p; });
             }
         } else {
 #pragma unroll
@@ -370,15 +380,14 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
         group_sync(gbar, TG);
         if (!PF && tl + tstep < tiles) {
             const float2 *gn = s + (insert_zeros((idx_t)(tl + tstep), d.ins_pos, d.nins) | dt);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const float2 x = gn[roff(j)];
+            gray_walk(gn, e, [&](int j, const float2 *p) {
+                const float2 x = *p;
                 v[2 * j] = __float_as_uint(x.x);
                 v[2 * j + 1] = __float_as_uint(x.y);
-            }
+            });
         }
 #pragma unroll
-        for (int j = 0; j < 32; ++j) gp[roff(j)] = tile_sm[pt ^ Swz<float>::f((unsigned)j << t)];
+        gray_walk(gp, e, [&](int j, float2 *p) { *p = tile_sm[pt ^ Swz<float>::f((unsigned)j << t)]; });
         group_sync(gbar, TG);  // the natural tile is read before the next splits
     }
     // A group whose bulk-copy wait never ran still owns an outstanding copy
