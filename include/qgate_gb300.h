@@ -147,10 +147,10 @@ int qg_set_fusion(int max_tile_lanes);
  * per-amplitude instruction budget that closes a stage early (0 = none). */
 int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budget);
 /* Extension: 1 runs large fused stages with the persistent, double-buffered
- * stage kernel (and 12-lane tensor-core stages with the variant that
- * prefetches each group's next tile into registers); 0 (default) with one
- * CTA per tile (tensor-core stages: four groups per SM), which keeps more
- * warps resident per SM. */
+ * stage kernel (and 12-lane tensor-core stages with two threads per tile
+ * row); 0 (default) with one CTA per tile (tensor-core stages: one thread
+ * per row), which keeps more warps resident per SM for the CUDA-core stage
+ * and fewer, busier threads for the tensor-core stage. */
 int qg_set_stage_pipelining(int on);
 /* Extension: 1 (default) runs complex64 stages of 12- or 13-lane tiles as
  * fused 5-lane blocks (32x32 complex matrices) on the tensor cores, 0 on the

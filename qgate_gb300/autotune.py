@@ -5,7 +5,7 @@ lanes, run by the register-resident stage kernel with `reg_lanes` lanes per
 thread's registers, and closes a stage when its estimated per-amplitude
 instruction count passes `cost_budget`; complex64 stages of 12 or 13 lanes
 can instead run on the tensor cores as fused 5-lane blocks (`tensor`), with
-or without the next-tile prefetch (`prefetch`).  Which shape is fastest
+one or two threads per tile row (`prefetch` = the stage-pipelining switch).  Which shape is fastest
 depends on the state size, the precision and the gate mix, so this module
 times a candidate grid on a caller-supplied circuit and keeps the best
 shape per (device, lanes, precision) in a JSON cache next to the package.

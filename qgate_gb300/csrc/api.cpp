@@ -503,23 +503,21 @@ struct TcLayout {
 };
 
 // Operand layout of a block (tile index -> operand slot; a slot is one
-// complex amplitude as f16x2), a bit permutation: amps[0..1] -> 0..1,
-// rows[0..2] -> 2..4, amps[2] -> 5, rows[3..6] -> 6..9, amps[3..4] ->
-// 10..11, rows[7] -> 12.  Slot bits 0..1 (with the complex part) span one
-// 16-byte core-matrix row along K, rows[0..2] the 8 rows of a core matrix,
-// amps[2] the second core matrix of an MMA's K = 16 (leading byte offset
-// 128), rows[3..6] the 8-row groups (stride byte offset 256), amps[3..4]
-// the K-step (4096 bytes per MMA), rows[7] the second 128-row group (16384
-// bytes).
+// complex amplitude as f16x2, 4 bytes): the canonical K-major layout with the
+// 128-byte swizzle.  Before the swizzle, row r of a 128-row group is 128
+// contiguous bytes (its 32 amplitudes: amps[0..4] -> slot bits 0..4), rows
+// r % 8 -> bits 5..7 (128 bytes apart), r / 8 -> bits 8..11 (8-row atoms of
+// 1024 bytes, the stride byte offset), rows[7] -> bit 12 (second 128-row
+// group, 16384 bytes); r's bits are rows[0..6].  The swizzle XORs the 16-byte
+// chunk index (slot bits 2..4) with r % 8 (slot bits 5..7).  All of it is a
+// GF(2)-linear map of the tile index.
 static unsigned tc_operand_slot(const TcLayout &L, unsigned tidx) {
-    static const int row_dst[8] = {2, 3, 4, 6, 7, 8, 9, 12};
-    static const int amp_dst[5] = {0, 1, 5, 10, 11};
-    unsigned out = 0;
-    for (int i = 0; i < 8; ++i)
-        if (L.rows[i] >= 0 && (tidx >> L.rows[i] & 1u)) out |= 1u << row_dst[i];
+    unsigned c = 0;
     for (int k = 0; k < 5; ++k)
-        if (tidx >> L.amps[k] & 1u) out |= 1u << amp_dst[k];
-    return out;
+        if (tidx >> L.amps[k] & 1u) c |= 1u << k;
+    for (int i = 0; i < 8; ++i)
+        if (L.rows[i] >= 0 && (tidx >> L.rows[i] & 1u)) c |= 1u << (i < 7 ? 5 + i : 12);
+    return c ^ (((c >> 5) & 7u) << 2);
 }
 
 template <class F> static SetSlots tc_slots(const TcLayout &src, int t, F dst) {
@@ -619,45 +617,56 @@ tc_blocks(const std::vector<const PendingGate *> &gates, const TileLanes &tl) {
 }
 
 // Orders a block's lanes and rows so that the stores into its operand hit
-// distinct banks: the bank of a 4-byte slot is its bits 0..4, which come
-// from amps[0..1] and rows[0..2], and a warp's threads differ in the source
-// layout's rows[0..4] (W); each W lane placed there doubles the banks hit.
-// So amps[0..1] are taken from W first, then rows[0..2]; rows[3..4] are
-// chosen so that the next block can do the same (two of this layout's
-// rows[0..4] among its lanes, three outside).
+// distinct banks.  The bank of a slot is bits 0..4 of tc_operand_slot:
+// amps[0], amps[1], amps[2] ^ rows[0], amps[3] ^ rows[1], amps[4] ^ rows[2];
+// a warp's threads differ in the source layout's rows[0..4] (W), so the
+// stores are conflict-free when W's lanes drive the five bank bits one each:
+// two W lanes of the block as amps[0..1], further W lanes of the block as
+// amps[2..4], and W's other lanes as the rows[k] whose amps[k + 2] is not a W
+// lane.  That works whenever the block holds at least two W lanes.  rows[3..4]
+// are then chosen so that the next block can do the same (at least two of
+// this layout's rows[0..4] among its lanes).
 static TcLayout tc_choose_layout(unsigned lanes, unsigned next_lanes, const TcLayout &src, int m) {
     unsigned W = 0;
     for (int x = 0; x < 5; ++x) W |= 1u << src.rows[x];
-    std::vector<int> L, R;
-    for (int p = 0; p < m; ++p) (lanes >> p & 1u ? L : R).push_back(p);
     auto in_w = [&](int p) { return (W >> p & 1u) != 0; };
-    std::stable_sort(L.begin(), L.end(), [&](int p, int q) { return in_w(p) && !in_w(q); });
-    // rows[0..2]: W lanes first; among equals, lanes outside the next block.
     auto nxt = [&](int p) { return (next_lanes >> p & 1u) != 0; };
-    std::stable_sort(R.begin(), R.end(), [&](int p, int q) {
-        if (in_w(p) != in_w(q)) return in_w(p);
-        return !nxt(p) && nxt(q);
-    });
+    std::vector<int> Lw, Lo, Rw, Ro;
+    for (int p = 0; p < m; ++p) {
+        if (lanes >> p & 1u) (in_w(p) ? Lw : Lo).push_back(p);
+        else (in_w(p) ? Rw : Ro).push_back(p);
+    }
+    // Rows outside W: lanes outside the next block first (they keep the next
+    // block's choice free); W rows: lanes of the next block last.
+    std::stable_sort(Ro.begin(), Ro.end(), [&](int p, int q) { return !nxt(p) && nxt(q); });
     TcLayout c;
     for (int x = 0; x < 8; ++x) c.rows[x] = -1;
-    for (int k = 0; k < 5; ++k) c.amps[k] = L[k];
-    for (int x = 0; x < 3; ++x) c.rows[x] = R[x];
-    int inext = 0;
-    for (int x = 0; x < 3; ++x) inext += nxt(c.rows[x]);
-    std::vector<int> rin, rout;
-    for (size_t x = 3; x < R.size(); ++x) (nxt(R[x]) ? rin : rout).push_back(R[x]);
-    std::vector<int> rest;
-    size_t pi = 0, po = 0;
-    for (int x = 0; x < 2; ++x) {
-        if ((inext < 2 && pi < rin.size()) || po >= rout.size()) {
-            rest.push_back(rin[pi++]);
-            ++inext;
+    // amps: W lanes first (the first two are amps[0..1]).
+    std::vector<int> A(Lw);
+    A.insert(A.end(), Lo.begin(), Lo.end());
+    for (int k = 0; k < 5; ++k) c.amps[k] = A[k];
+    // rows[0..2]: a W row where amps[k + 2] is not a W lane, else a non-W row.
+    size_t iw = 0, io = 0;
+    std::vector<bool> used_o(Ro.size(), false);
+    for (int k = 0; k < 3; ++k) {
+        if (!in_w(c.amps[k + 2]) && iw < Rw.size()) {
+            c.rows[k] = Rw[iw++];
+        } else if (io < Ro.size()) {
+            used_o[io] = true;
+            c.rows[k] = Ro[io++];
         } else {
-            rest.push_back(rout[po++]);
+            c.rows[k] = Rw[iw++];
         }
     }
-    while (pi < rin.size()) rest.push_back(rin[pi++]);
-    while (po < rout.size()) rest.push_back(rout[po++]);
+    std::vector<int> rest;
+    for (; iw < Rw.size(); ++iw) rest.push_back(Rw[iw]);
+    for (size_t x = io; x < Ro.size(); ++x) rest.push_back(Ro[x]);
+    // rows[3..4]: top up to two lanes of the next block among rows[0..4].
+    int inext = 0;
+    for (int x = 0; x < 3; ++x) inext += nxt(c.rows[x]);
+    std::stable_sort(rest.begin(), rest.end(), [&](int p, int q) {
+        return inext < 2 ? (nxt(p) && !nxt(q)) : (!nxt(p) && nxt(q));
+    });
     for (size_t x = 0; x < rest.size(); ++x) c.rows[3 + x] = rest[x];
     return c;
 }
@@ -687,11 +696,135 @@ static void tc_block_matrix(const std::vector<const PendingGate *> &gates, const
     }
 }
 
+// Fills a block of fewer than 5 lanes: lanes of the source layout's warp
+// bits first (two of them keep its operand stores conflict-free), then the
+// lowest free positions.
+static unsigned tc_fill_lanes(unsigned lanes, const TcLayout &src, int m) {
+    for (int x = 0; x < 5 && __builtin_popcount(lanes) < 5; ++x) {
+        unsigned in_warp = 0;
+        for (int y = 0; y < 5; ++y) in_warp += lanes >> src.rows[y] & 1u;
+        if (in_warp >= 2) break;
+        lanes |= 1u << src.rows[x];
+    }
+    for (int p = 0; p < m && __builtin_popcount(lanes) < 5; ++p) lanes |= 1u << p;
+    return lanes;
+}
+
+// Shared-memory wavefronts of one warp-wide 4-byte store through slot
+// tables: the largest number of threads on one bank.
+static int tc_store_cost(const SetSlots &ss) {
+    int cnt[32] = {0};
+    int mx = 0;
+    for (int i = 0; i < 32; ++i) mx = std::max(mx, ++cnt[ss.lo[i] & 31]);
+    return mx;
+}
+
+// Wavefronts of one warp-wide 8-byte store through slot tables (two half
+// warps; per half, the largest number of threads on one 8-byte bank pair).
+static int tc_store_cost8(const SetSlots &ss) {
+    int cost = 0;
+    for (int h = 0; h < 2; ++h) {
+        int cnt[16] = {0}, mx = 0;
+        for (int i = 0; i < 16; ++i) mx = std::max(mx, ++cnt[ss.lo[16 * h + i] & 15]);
+        cost += mx;
+    }
+    return cost;
+}
+
+// Host plan of one tensor-stage launch: blocks [b0, b0 + nb) of a stage on
+// tile `tl` -> the descriptor (all but the operand pointer) and the split
+// block operands (nb x 2 x 4096 FP16 values) in `ops`.
+static void tc_plan_launch(const TileLanes &tl, int n,
+                           const std::vector<std::pair<unsigned, std::vector<const PendingGate *>>> &blocks,
+                           size_t b0, int nb, TcStageDesc &desc, unsigned short *ops) {
+    const int m = (int)tl.lanes.size();
+    const int t = m - 5;
+    const size_t kBlockHalves = 2 * 64 * 64;
+    memset(&desc, 0, sizeof(desc));
+    desc.n = n;
+    desc.m = m;
+    desc.nins = m < n ? m : 0;
+    for (int j = 0; j < desc.nins; ++j) desc.ins_pos[j] = tl.lanes[j];
+    desc.nblocks = nb;
+    // Load layout: tile positions 0..3 (the contiguous low lanes) plus one
+    // more position p on the warp's thread bits, chosen so that the first
+    // block's operand stores hit the fewest banks twice.
+    auto load_layout = [&](int p) {
+        TcLayout L;
+        for (int i = 0; i < 8; ++i) L.rows[i] = -1;
+        int r = 0, a = 0;
+        for (int q = 0; q < 4; ++q) L.rows[r++] = q;
+        L.rows[r++] = p;
+        for (int q = 4; q < m; ++q) {
+            if (q == p) continue;
+            if (a < 5) L.amps[a++] = q;
+            else L.rows[r++] = q;
+        }
+        return L;
+    };
+    TcLayout cur = load_layout(4);
+    {
+        unsigned lanes0 = tc_fill_lanes(blocks[b0].first, cur, m);
+        const unsigned next0 = nb > 1 ? blocks[b0 + 1].first : 0u;
+        int best = 1 << 30;
+        for (int p = 4; p < m; ++p) {
+            TcLayout L = load_layout(p);
+            unsigned l0 = tc_fill_lanes(blocks[b0].first, L, m);
+            TcLayout lay = tc_choose_layout(l0, next0, L, m);
+            int c = tc_store_cost(tc_slots(L, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); }));
+            if (c < best) {
+                best = c;
+                cur = L;
+                lanes0 = l0;
+            }
+        }
+        (void)lanes0;
+    }
+    for (int b = 0; b < t; ++b) desc.row_lane[b] = tl.lanes[cur.rows[b]];
+    for (int j = 0; j < 32; ++j) {
+        long long off = 0;
+        for (int k = 0; k < 5; ++k)
+            if (j >> k & 1) off |= 1LL << tl.lanes[cur.amps[k]];
+        desc.dep_hi[j] = off;
+    }
+    desc.sets[nb + 1] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
+    std::complex<double> U[1024];
+    for (int b = 0; b < nb; ++b) {
+        unsigned lanes = blocks[b0 + b].first;
+        lanes = tc_fill_lanes(lanes, cur, m);
+        const unsigned next = b + 1 < nb ? blocks[b0 + b + 1].first : 0u;
+        TcLayout lay = tc_choose_layout(lanes, next, cur, m);
+        if (b + 1 == nb) {
+            // Last block: rows[3..4] only feed the 8-byte stores into the
+            // natural tile; pick them for the fewest wavefronts there.
+            int best = 1 << 30;
+            TcLayout keep = lay;
+            for (int x = 3; x < t; ++x)
+                for (int y = 3; y < t; ++y) {
+                    if (x == y) continue;
+                    TcLayout c = keep;
+                    std::swap(c.rows[3], c.rows[x]);
+                    std::swap(c.rows[4], c.rows[y == 3 ? x : y]);
+                    const int cost = tc_store_cost8(
+                        tc_slots(c, t, [&](unsigned ti) { return host_swz(ti, kFP32); }));
+                    if (cost < best) {
+                        best = cost;
+                        lay = c;
+                    }
+                }
+        }
+        desc.sets[b] = tc_slots(cur, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); });
+        tc_block_matrix(blocks[b0 + b].second, tl, lay, U);
+        tc_operand(U, ops + b * kBlockHalves, ops + b * kBlockHalves + kBlockHalves / 2);
+        cur = lay;
+    }
+    desc.sets[nb] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
+}
+
 static void run_tstage(Device &d, States *s, const TileLanes &tl,
                        const std::vector<const PendingGate *> &gates) {
     const int n = s->n_lanes;
     const int m = (int)tl.lanes.size();
-    const int t = m - 5;
     auto blocks = tc_blocks(gates, tl);
     if (!d.h_bring) {
         QG_CUDA(cudaMallocHost(&d.h_bring, Device::kBRingBytes));
@@ -710,38 +843,8 @@ static void run_tstage(Device &d, States *s, const TileLanes &tl,
         unsigned short *hb = d.h_bring + d.bring_off / sizeof(unsigned short);
         unsigned short *db = d.d_bring + d.bring_off / sizeof(unsigned short);
         static TcStageDesc desc;
-        memset(&desc, 0, sizeof(desc));
-        desc.n = n;
-        desc.m = m;
-        long long dep[32];
-        fill_tile_header(tl, n, 5, desc.lowrun, desc.nhi, desc.hi_pos, desc.nins, desc.ins_pos,
-                         dep);
-        for (int i = 0; i < 32; ++i) desc.dep_hi[i] = dep[i];
-        desc.nblocks = nb;
+        tc_plan_launch(tl, n, blocks, b0, nb, desc, hb);
         desc.bmats = db;
-        TcLayout cur;
-        for (int i = 0; i < 8; ++i) cur.rows[i] = i < t ? i : -1;
-        for (int k = 0; k < 5; ++k) cur.amps[k] = t + k;
-        std::complex<double> U[1024];
-        for (int b = 0; b < nb; ++b) {
-            unsigned lanes = blocks[b0 + b].first;
-            // Fill a block of fewer than 5 lanes with lanes of the source
-            // warp bits first (two of them keep its stores conflict-free).
-            for (int x = 0; x < 5 && __builtin_popcount(lanes) < 5; ++x) {
-                unsigned in_warp = 0;
-                for (int y = 0; y < 5; ++y) in_warp += lanes >> cur.rows[y] & 1u;
-                if (in_warp >= 2) break;
-                lanes |= 1u << cur.rows[x];
-            }
-            for (int p = 0; p < m && __builtin_popcount(lanes) < 5; ++p) lanes |= 1u << p;
-            const unsigned next = b + 1 < nb ? blocks[b0 + b + 1].first : 0u;
-            TcLayout lay = tc_choose_layout(lanes, next, cur, m);
-            desc.sets[b] = tc_slots(cur, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); });
-            tc_block_matrix(blocks[b0 + b].second, tl, lay, U);
-            tc_operand(U, hb + b * kBlockHalves, hb + b * kBlockHalves + kBlockHalves / 2);
-            cur = lay;
-        }
-        desc.sets[nb] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
         QG_CUDA(cudaMemcpyAsync(db, hb, bytes, cudaMemcpyHostToDevice, d.stream));
         d.bring_off += bytes;
         timed(d, "tstage", [&] { launch_tstage(s->d, desc, d.stream, d.pipelined); });

@@ -138,26 +138,27 @@ template <class R> struct RStageDesc {
 };
 
 // Tensor-core stage (complex64): fused 5-lane blocks applied as tcgen05
-// products to a tile of m = 12 or 13 lanes.  sets[b] maps the registers of
-// the layout before block b (the load layout for b = 0) to the slots of block
-// b's operand layout; sets[nblocks] maps the last block's layout to the
-// swizzled natural tile.  bmats holds per block the split operands Bh, Bl
-// (2 x 4096 FP16 values, canonical K-major layout).
+// products to a tile of m = 12 or 13 lanes.  Load layout: thread bit b holds
+// global lane row_lane[b], register bit k global lane log2(dep_hi[1 << k]).
+// sets[b] maps the registers of the layout before block b (the load layout
+// for b = 0) to the slots of block b's operand layout; sets[nblocks] maps the
+// last block's layout, sets[nblocks + 1] the load layout, to the swizzled
+// natural tile.  bmats holds per block the split operands Bh, Bl (2 x 4096
+// FP16 values, canonical K-major layout).
 constexpr int kMaxTcBlocks = 24;
 struct TcStageDesc {
     int n, m;
-    int lowrun, nhi;
-    int hi_pos[kMaxTileLanes];
+    int row_lane[8];
     int nins;
     int ins_pos[kMaxTileLanes];
     long long dep_hi[32];
     int nblocks;
     const unsigned short *bmats;
-    SetSlots sets[kMaxTcBlocks + 1];
+    SetSlots sets[kMaxTcBlocks + 2];
 };
-// prefetch: the 12-lane variant whose groups load their next tile while
-// running the current one.
-void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool prefetch);
+// two_per_row: the 12-lane variant with two threads per tile row (twice the
+// warps per SM, half the registers per thread).
+void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool two_per_row);
 // Blocks one tensor-stage launch holds (its operands stay in shared memory).
 int tstage_max_blocks(int m);
 // Status word of the tensor stage kernels (nonzero: a bounded wait gave up).

@@ -19,7 +19,8 @@
 //
 // Data path per block: thread r holds row r of the previous layout in
 // registers (64 floats); it splits each amplitude and stores Ah/Al straight
-// into the block's canonical no-swizzle K-major operand layout - the map from
+// into the block's canonical 128-byte-swizzled K-major operand layout (B:
+// no swizzle, written on the host) - the map from
 // (row, register) to operand slot is GF(2)-linear, so it is a precomputed
 // slot table (SetSlots), and no separate transpose pass exists.  One thread
 // issues the 12 MMAs per 128 rows and commits them to an mbarrier; every
@@ -51,11 +52,13 @@ __device__ __forceinline__ unsigned smem_u32(const void *p) {
 }
 
 // Shared-memory matrix descriptor: start address, leading-dimension byte
-// offset (between core matrices along K), stride-dimension byte offset
-// (between 8-row groups), descriptor version 1, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
+// offset (between core matrices along K; unused by swizzled K-major
+// layouts), stride-dimension byte offset (between 8-row groups), descriptor
+// version 1, layout type (0 = no swizzle, 2 = 128-byte swizzle).
+__device__ __forceinline__ uint64_t smem_desc(unsigned saddr, unsigned lbo, unsigned sbo,
+                                              unsigned layout = 0) {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
-           ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+           ((uint64_t)(sbo >> 4) << 32) | (1ull << 46) | ((uint64_t)layout << 61);
 }
 
 // Instruction descriptor of kind::f16: D = F32, A = B = F16, both K-major,
@@ -85,16 +88,19 @@ __device__ __forceinline__ void mbar_arrive(unsigned bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
 }
 
-// Bounded wait for the completion of the phase with the given parity.
+// Bounded wait for the completion of the phase with the given parity.  Each
+// try suspends the thread until the phase completes or a 20 us hint runs
+// out, so waiting threads do not spin on the issue slots; at most 2^16
+// tries (about 1.3 s).
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-    for (int i = 0; i < (1 << 20); ++i) {
+    for (int i = 0; i < (1 << 16); ++i) {
         unsigned ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(ok)
-            : "r"(bar), "r"(parity)
+            : "r"(bar), "r"(parity), "r"(20000u)
             : "memory");
         if (ok) return true;
     }
@@ -122,6 +128,16 @@ __device__ __forceinline__ void tmem_ld_x64(unsigned taddr, unsigned (&u)[64]) {
         : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld_x32(unsigned taddr, unsigned (&u)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]),
+          "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]),
+          "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31])
+        : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
@@ -141,18 +157,27 @@ __device__ __forceinline__ void split_f16x2(float x, float y, unsigned &hi, unsi
         : "f"(x), "f"(y));
 }
 
-// Visits the 32 registers of a thread in Gray-code order: f(j, p) with p =
-// base + offset of register j, where register j's offset is the sum of e[k]
-// over the set bits k of j.
-template <class P, class F>
+// Bit in which the Gray codes of i - 1 and i differ (ctz(i)), at compile
+// time once the loops are unrolled.
+__host__ __device__ constexpr int gray_bit(int i) {
+    return (i & 1) ? 0 : (i & 2) ? 1 : (i & 4) ? 2 : (i & 8) ? 3 : 4;
+}
+// Inverse Gray code of j (5 bits).
+__host__ __device__ constexpr int gray_index(int j) {
+    return j ^ (j >> 1) ^ (j >> 2) ^ (j >> 3) ^ (j >> 4);
+}
+
+// Visits the 2^NB registers of a thread in Gray-code order: f(j, p) with
+// p = base + offset of register j, where register j's offset is the sum of
+// e[k] over the set bits k of j.
+template <int NB, class P, class F>
 __device__ __forceinline__ void gray_walk(P *base, const long long (&e)[5], F f) {
     P *p = base;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
+    for (int i = 0; i < (1 << NB); ++i) {
         const int j = i ^ (i >> 1);
         if (i > 0) {
-            // gray(i) and gray(i - 1) differ in bit ctz(i)
-            const int k = (i & 1) ? 0 : (i & 2) ? 1 : (i & 4) ? 2 : (i & 8) ? 3 : 4;
+            const int k = gray_bit(i);
             p = (j >> k & 1) ? p + e[k] : p - e[k];
         }
         f(j, p);
@@ -169,26 +194,29 @@ __device__ __forceinline__ void group_sync(unsigned id, unsigned threads) {
 }
 
 // Persistent kernel, one CTA per SM.  The CTA holds every block operand of
-// the stage in shared memory (loaded once) and G independent tile groups of
-// 128 * RT threads (RT = 128-row groups per tile: tile lanes m = 12 for
-// RT = 1, 13 for RT = 2); each group walks its own tiles with its own
-// operand buffers, tensor-memory columns and mbarrier, so the groups overlap
-// one another's loads, splits and products on the SM's tensor core.
-//
-// PF: each group loads its next tile into registers while it runs the
-// blocks of the current one (64 more registers per thread, so fewer groups).
-template <int RT, int G, bool PF>
-__global__ void __launch_bounds__(128 * RT * G, 1)
+// the stage in shared memory (loaded once) and G independent tile groups;
+// each group walks its own tiles with its own operand buffers, tensor-memory
+// columns and mbarrier, so the groups overlap one another's loads, splits
+// and products on the SM's tensor core.  RT = 128-row groups per tile (tile
+// lanes m = 12 for RT = 1, 13 for RT = 2); H = threads per row (each thread
+// holds 32 / H amplitudes of its row; H = 2 halves the registers per thread
+// so that twice the warps fit).
+template <int RT, int G, int H>
+__global__ void __launch_bounds__(128 * RT * G * H, 1)
 k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long long tiles) {
     constexpr int m = RT == 1 ? 12 : 13;
     constexpr int t = m - 5;
-    constexpr unsigned TG = 128u * RT;                  // threads per group
+    constexpr int NA = 32 / H;                          // amplitudes per thread
+    constexpr int NB = H == 1 ? 5 : 4;                  // register bits per thread
+    constexpr unsigned TR = 128u * RT;                  // rows per tile
+    constexpr unsigned TG = TR * H;                     // threads per group
     constexpr unsigned T = TG * G;
     constexpr unsigned kColsGroup = 64u * RT;
     constexpr unsigned kCols = kColsGroup * G <= 32 ? 32 : (kColsGroup * G <= 64 ? 64 :
                                (kColsGroup * G <= 128 ? 128 : (kColsGroup * G <= 256 ? 256 : 512)));
     constexpr unsigned kBBytes = 2u * 64u * 64u * 2u;   // Bh, Bl of one block in FP16
     constexpr unsigned kABytes = 4u << m;               // one FP16 operand of a tile
+    static_assert(H == 1 || H == 2, "threads per row");
     extern __shared__ __align__(1024) unsigned char smraw[];
     const int nb = d.nblocks;
     unsigned char *Bs = smraw + (size_t)G * 2 * kABytes;
@@ -199,10 +227,17 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
     const unsigned tid = threadIdx.x;
     const unsigned warp = tid >> 5;
     const unsigned g = tid / TG, lt = tid % TG;
+    const unsigned r = lt % TR, hh = lt / TR;           // row, half of the row
+    const unsigned wg = (lt >> 5) % (4u * RT);          // warp within the rows
     unsigned *Ah = (unsigned *)(smraw + (size_t)g * 2 * kABytes);  // f16x2 per amplitude
     unsigned *Al = Ah + (1 << m);
     float2 *tile_sm = (float2 *)Ah;                     // natural tile (aliases Ah, Al)
 
+    // The operand atoms must be 1024-byte aligned for the 128-byte swizzle.
+    if ((smem_u32(smraw) & 1023u) != 0u) {
+        if (tid == 0) atomicOr(&g_tc_status, 4u);
+        return;
+    }
     if (tid == 0) abort_sh[0] = *(volatile unsigned *)&g_tc_status != 0u;
     __syncthreads();
     if (abort_sh[0]) return;
@@ -224,12 +259,13 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
         mbar_init(bb, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    rs::copy_sets(sset, d.sets, nb + 1, tid, T);
+    rs::copy_sets(sset, d.sets, nb + 2, tid, T);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const unsigned tmem = tmem_sh + g * kColsGroup + 64u * ((warp >> 2) % RT) +
-                          ((32u * (warp & 3u)) << 16);    // this warp's lanes and columns
+    // This warp's lanes (row quadrant) and columns (128-row group, half).
+    const unsigned tmem = tmem_sh + g * kColsGroup + 64u * (wg >> 2) + 32u * hh +
+                          ((32u * (wg & 3u)) << 16);
     const unsigned dcol0 = tmem_sh + g * kColsGroup;       // the group's accumulator
     if (tid == 0) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bb),
@@ -243,72 +279,57 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
                 : "memory");
     }
 
-    // Load layout: thread r = tile lanes 0..t-1, register j = tile lanes t..m-1.
-    const int lr = d.lowrun < t ? d.lowrun : t;
-    idx_t dt = (idx_t)(lt & ((1u << lr) - 1u));
-    for (int b = lr; b < t; ++b)
-        if (lt & (1u << b)) dt |= 1LL << d.hi_pos[b - d.lowrun];
-    const unsigned pt = Swz<float>::f(lt);
-    // Global offset of register j: the sum (the bits are disjoint) of e[k]
-    // over the set bits k of j.  The loops below visit j in Gray-code order,
-    // so each step adds or subtracts one e[k] from a running pointer.
+    // Load layout: row bit b at global lane row_lane[b], amplitude bit k at
+    // the lane of e[k] (chosen per stage on the host; lanes 0..3 of the tile
+    // are among the warp's row bits, so accesses come in 128-byte runs).  A
+    // thread holds amplitudes hh * NA + j of its row, j < NA.
     long long e[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) e[k] = d.dep_hi[1 << k];
+    idx_t dt = 0;
+    for (int b = 0; b < t; ++b)
+        if (r & (1u << b)) dt |= 1LL << d.row_lane[b];
+    if (H == 2 && hh) dt += e[4];
+    // Slots of the load layout in the swizzled natural tile (copy-out).
+    const SetSlots &nat = sset[nb + 1];
+    unsigned pt = (unsigned)nat.lo[r & 31u] ^ (unsigned)nat.hi[r >> 5];
+    if (H == 2 && hh) pt ^= nat.q[4];
+    unsigned qn[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) qn[k] = nat.q[k];
     const unsigned gbar = 1u + g;                          // the group's named barrier
     unsigned phase = 0;
     bool ok = true, b_ready = false;
-
     const long long tstep = (long long)gridDim.x * G;
-    float2 w[PF ? 32 : 1];
-    if (PF) {
-        const long long tl0 = (long long)blockIdx.x * G + g;
-        if (tl0 < tiles) {
-            const float2 *gp0 = s + (insert_zeros((idx_t)tl0, d.ins_pos, d.nins) | dt);
-            gray_walk(gp0, e, [&](int j, const float2 *p) { w[PF ? j : 0] = *p; });
-        }
-    }
-    // Without PF the next tile's loads are issued into v once the finished
-    // tile has been staged in shared memory, before it is copied out, so
-    // they are in flight during the copy-out; the scale is applied after.
-    unsigned v[64];  // floats (bits): row lt of the current layout
-    if (!PF) {
-        const long long tl0 = (long long)blockIdx.x * G + g;
-        if (tl0 < tiles) {
-            const float2 *gp0 = s + (insert_zeros((idx_t)tl0, d.ins_pos, d.nins) | dt);
-            gray_walk(gp0, e, [&](int j, const float2 *p) {
-                const float2 x = *p;
-                v[2 * j] = __float_as_uint(x.x);
-                v[2 * j + 1] = __float_as_uint(x.y);
-            });
-        }
-    }
+
+    // The next tile's loads are issued into v once the finished tile has
+    // been staged in shared memory, before it is copied out, so they are in
+    // flight during the copy-out; the scale is applied after.
+    unsigned v[2 * NA];  // floats (bits): this thread's part of row r
+    auto load_raw = [&](long long tl) {
+        const float2 *gp0 = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
+        gray_walk<NB>(gp0, e, [&](int j, const float2 *p) {
+            const float2 x = *p;
+            v[2 * j] = __float_as_uint(x.x);
+            v[2 * j + 1] = __float_as_uint(x.y);
+        });
+    };
+    if ((long long)blockIdx.x * G + g < tiles) load_raw((long long)blockIdx.x * G + g);
     for (long long tl = (long long)blockIdx.x * G + g; tl < tiles && ok; tl += tstep) {
         float2 *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
-        if (PF) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                v[2 * j] = __float_as_uint(w[PF ? j : 0].x * kScale);
-                v[2 * j + 1] = __float_as_uint(w[PF ? j : 0].y * kScale);
-            }
-            if (tl + tstep < tiles) {
-                const float2 *gn =
-                    s + (insert_zeros((idx_t)(tl + tstep), d.ins_pos, d.nins) | dt);
-                gray_walk(gn, e, [&](int j, const float2 *p) { w[PF ? j : 0] = *p; });
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < 64; ++i) v[i] = __float_as_uint(__uint_as_float(v[i]) * kScale);
-        }
+        for (int i = 0; i < 2 * NA; ++i) v[i] = __float_as_uint(__uint_as_float(v[i]) * kScale);
         for (int b = 0; b < nb; ++b) {
             const SetSlots &ss = sset[b];
-            const unsigned base = (unsigned)ss.lo[lt & 31u] ^ (unsigned)ss.hi[lt >> 5];
-            unsigned q[5];
+            unsigned slot = (unsigned)ss.lo[r & 31u] ^ (unsigned)ss.hi[r >> 5];
+            if (H == 2 && hh) slot ^= ss.q[4];
+            unsigned q[NB];
 #pragma unroll
-            for (int k = 0; k < 5; ++k) q[k] = ss.q[k];
+            for (int k = 0; k < NB; ++k) q[k] = ss.q[k];
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const unsigned slot = reg_slot<5>(base, q, j);
+            for (int i = 0; i < NA; ++i) {  // Gray-code order: one XOR per slot
+                const int j = i ^ (i >> 1);
+                if (i > 0) slot ^= q[gray_bit(i)];
                 unsigned h, l;
                 split_f16x2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]), h, l);
                 Ah[slot] = h;
@@ -326,9 +347,11 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
                     for (int mt = 0; mt < RT; ++mt) {
 #pragma unroll
                         for (int ks = 0; ks < 4; ++ks) {
-                            const unsigned aoff = 16384u * mt + 4096u * ks, boff = 2048u * ks;
-                            const uint64_t dah = smem_desc(ah + aoff, 128, 256);
-                            const uint64_t dal = smem_desc(al + aoff, 128, 256);
+                            // A: 128-byte swizzled K-major, 8-row atoms of
+                            // 1024 bytes, K-step ks at +32 bytes in the atom.
+                            const unsigned aoff = 16384u * mt + 32u * ks, boff = 2048u * ks;
+                            const uint64_t dah = smem_desc(ah + aoff, 16, 1024, 2);
+                            const uint64_t dal = smem_desc(al + aoff, 16, 1024, 2);
                             const uint64_t dbh = smem_desc(bh + boff, 1024, 128);
                             const uint64_t dbl = smem_desc(bl + boff, 1024, 128);
                             const unsigned dcol = dcol0 + 64u * mt;
@@ -358,7 +381,10 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
                 break;
             }
             tc_fence_after();
-            tmem_ld_x64(tmem, v);
+            if constexpr (H == 1)
+                tmem_ld_x64(tmem, v);
+            else
+                tmem_ld_x32(tmem, v);
             tmem_wait_ld();
         }
         tc_fence_before();
@@ -367,27 +393,29 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
         // Last layout -> swizzled natural tile -> load layout -> global.
         {
             const SetSlots &ss = sset[nb];
-            const unsigned base = (unsigned)ss.lo[lt & 31u] ^ (unsigned)ss.hi[lt >> 5];
-            unsigned q[5];
+            unsigned slot = (unsigned)ss.lo[r & 31u] ^ (unsigned)ss.hi[r >> 5];
+            if (H == 2 && hh) slot ^= ss.q[4];
+            unsigned q[NB];
 #pragma unroll
-            for (int k = 0; k < 5; ++k) q[k] = ss.q[k];
+            for (int k = 0; k < NB; ++k) q[k] = ss.q[k];
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-                tile_sm[reg_slot<5>(base, q, j)] =
-                    make_float2(__uint_as_float(v[2 * j]) * kUnscale,
-                                __uint_as_float(v[2 * j + 1]) * kUnscale);
+            for (int i = 0; i < NA; ++i) {
+                const int j = i ^ (i >> 1);
+                if (i > 0) slot ^= q[gray_bit(i)];
+                tile_sm[slot] = make_float2(__uint_as_float(v[2 * j]) * kUnscale,
+                                            __uint_as_float(v[2 * j + 1]) * kUnscale);
+            }
         }
         group_sync(gbar, TG);
-        if (!PF && tl + tstep < tiles) {
-            const float2 *gn = s + (insert_zeros((idx_t)(tl + tstep), d.ins_pos, d.nins) | dt);
-            gray_walk(gn, e, [&](int j, const float2 *p) {
-                const float2 x = *p;
-                v[2 * j] = __float_as_uint(x.x);
-                v[2 * j + 1] = __float_as_uint(x.y);
+        if (tl + tstep < tiles) load_raw(tl + tstep);
+        {
+            unsigned slot = pt;
+            gray_walk<NB>(gp, e, [&](int j, float2 *p) {
+                const int i = gray_index(j);
+                if (i > 0) slot ^= qn[gray_bit(i)];
+                *p = tile_sm[slot];
             });
         }
-#pragma unroll
-        gray_walk(gp, e, [&](int j, float2 *p) { *p = tile_sm[pt ^ Swz<float>::f((unsigned)j << t)]; });
         group_sync(gbar, TG);  // the natural tile is read before the next splits
     }
     // A group whose bulk-copy wait never ran still owns an outstanding copy
@@ -407,21 +435,21 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
 // stage's block operands and the slot tables.
 static size_t tstage_smem(int m, int groups, int nblocks) {
     return (size_t)groups * 2 * ((size_t)4 << m) + (size_t)nblocks * 2 * 64 * 64 * 2 +
-           sizeof(SetSlots) * (size_t)(nblocks + 1);
+           sizeof(SetSlots) * (size_t)(nblocks + 2);
 }
 
-// Groups per CTA: 12-lane tiles 4 groups of 128 threads (3 with the
-// next-tile prefetch), 13-lane tiles 2 groups of 256 threads.
-static int tstage_groups(int m, bool prefetch) { return m == 12 ? (prefetch ? 3 : 4) : 2; }
+// Groups per CTA: 4 for 12-lane tiles (of 128 threads, or of 256 with two
+// threads per row), 2 of 256 threads for 13-lane tiles.
+static int tstage_groups(int m) { return m == 12 ? 4 : 2; }
 
 int tstage_max_blocks(int m) {
-    const int groups = tstage_groups(m, false);
+    const int groups = tstage_groups(m);
     int nb = 1;
     while (nb < kMaxTcBlocks && tstage_smem(m, groups, nb + 1) + 2048 <= 227 * 1024) ++nb;
     return nb;
 }
 
-void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool prefetch) {
+void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool two_per_row) {
     if (d.m != 12 && d.m != 13) fail(2, "tensor stage: tile lanes must be 12 or 13 (got %d)", d.m);
     if (d.nblocks < 1 || d.nblocks > tstage_max_blocks(d.m))
         fail(2, "tensor stage: bad block count %d", d.nblocks);
@@ -436,12 +464,12 @@ void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool 
         const long long ctas = std::min<long long>((tiles + groups - 1) / groups, sms);
         kern<<<(unsigned)ctas, threads, smem, stream>>>((float2 *)state, d, tiles);
     };
-    if (d.m == 12 && prefetch)
-        launch(k_tstage<1, 3, true>, 3, 384);
+    if (d.m == 12 && two_per_row)
+        launch(k_tstage<1, 4, 2>, 4, 1024);
     else if (d.m == 12)
-        launch(k_tstage<1, 4, false>, 4, 512);
+        launch(k_tstage<1, 4, 1>, 4, 512);
     else
-        launch(k_tstage<2, 2, false>, 2, 512);
+        launch(k_tstage<2, 2, 1>, 2, 512);
     QG_CUDA(cudaGetLastError());
 }
 

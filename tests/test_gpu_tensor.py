@@ -116,10 +116,10 @@ def test_tensor_stage_matches_cuda_core_stage(rt, tensor_mode):
     assert nat.tensor_stage_status() == 0
 
 
-def test_tensor_stage_prefetch_variant(rt, tensor_mode):
-    """The 12-lane variant whose groups prefetch their next tile into
-    registers (selected with stage pipelining on) against the oracle and
-    against the default variant (same arithmetic: identical results)."""
+def test_tensor_stage_two_threads_per_row_variant(rt, tensor_mode):
+    """The 12-lane variant with two threads per tile row (selected with stage
+    pipelining on) against the oracle and against the default variant (same
+    arithmetic: identical results)."""
     nat = tensor_mode
     nat.set_fusion_params(nat.PREC_FP32, 12, 5, 0)
     rng = np.random.default_rng(18)
