@@ -589,6 +589,33 @@ static void tc_operand(const std::complex<double> *U, unsigned short *bh, unsign
         }
 }
 
+// Bias compensation for the tensor core's accumulator.  The FP32 accumulator
+// of tcgen05.mma rounds toward zero at every MMA, so each output shrinks in
+// magnitude by half an ulp per rounding on average; the kernel orders the
+// MMAs so that only the main product's K-steps round at full magnitude, and
+// an output whose inputs span c of the four K-steps sees roundings at about
+// 1/c, 2/c, ..., 1 of its final value: an expected relative shrink of
+// (c + 1) / 4 * kRzShrink, kRzShrink being the mean relative shrink of one
+// rounding at full magnitude (measured on GB300 from the norm drift of
+// dense blocks: 7.25e-8 per block for c = 4).  Each row of U is scaled up by
+// that amount, which removes the drift (it would otherwise shrink the norm by
+// ~1.5e-7 per block); the remaining error is unbiased.
+constexpr double kRzShrink = 5.8e-8;
+
+static void tc_compensate(std::complex<double> *U) {
+    for (int o = 0; o < 32; ++o) {
+        int c = 0;
+        for (int ks = 0; ks < 4; ++ks) {
+            bool nz = false;
+            for (int i = 8 * ks; i < 8 * ks + 8; ++i) nz |= U[o * 32 + i] != 0.;
+            c += nz;
+        }
+        if (c == 0) continue;
+        const double f = 1. + 0.25 * (c + 1) * kRzShrink;
+        for (int i = 0; i < 32; ++i) U[o * 32 + i] *= f;
+    }
+}
+
 // Greedy 5-lane blocks over a stage's gates in order: a gate joins the open
 // block when its lanes fit and no earlier deferred gate shares a lane (so it
 // commutes with everything deferred); the rest start the next block.
@@ -815,6 +842,7 @@ static void tc_plan_launch(const TileLanes &tl, int n,
         }
         desc.sets[b] = tc_slots(cur, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); });
         tc_block_matrix(blocks[b0 + b].second, tl, lay, U);
+        tc_compensate(U);
         tc_operand(U, ops + b * kBlockHalves, ops + b * kBlockHalves + kBlockHalves / 2);
         cur = lay;
     }

@@ -343,8 +343,15 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
                     tc_fence_after();
                     const unsigned ah = smem_u32(Ah), al = smem_u32(Al),
                                    bh = smem_u32(Bs + (size_t)b * kBBytes), bl = bh + kBBytes / 2;
+                    // The tensor core rounds its FP32 accumulator toward zero
+                    // at every MMA, which shrinks magnitudes: the correction
+                    // products go first (small values), the main product's
+                    // four K-steps last, so that only those round at full
+                    // magnitude (the host scales each block's rows to cancel
+                    // the expected shrink of those four roundings).
 #pragma unroll
                     for (int mt = 0; mt < RT; ++mt) {
+                        const unsigned dcol = dcol0 + 64u * mt;
 #pragma unroll
                         for (int ks = 0; ks < 4; ++ks) {
                             // A: 128-byte swizzled K-major, 8-row atoms of
@@ -354,10 +361,14 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
                             const uint64_t dal = smem_desc(al + aoff, 16, 1024, 2);
                             const uint64_t dbh = smem_desc(bh + boff, 1024, 128);
                             const uint64_t dbl = smem_desc(bl + boff, 1024, 128);
-                            const unsigned dcol = dcol0 + 64u * mt;
-                            mma_f16(dcol, dah, dbh, ks > 0 ? 1u : 0u);
-                            mma_f16(dcol, dah, dbl, 1u);
+                            mma_f16(dcol, dah, dbl, ks > 0 ? 1u : 0u);
                             mma_f16(dcol, dal, dbh, 1u);
+                        }
+#pragma unroll
+                        for (int ks = 0; ks < 4; ++ks) {
+                            const unsigned aoff = 16384u * mt + 32u * ks, boff = 2048u * ks;
+                            mma_f16(dcol, smem_desc(ah + aoff, 16, 1024, 2),
+                                    smem_desc(bh + boff, 1024, 128), 1u);
                         }
                     }
                     mma_commit(bmma);

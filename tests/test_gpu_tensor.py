@@ -133,3 +133,39 @@ def test_tensor_stage_two_threads_per_row_variant(rt, tensor_mode):
     _check(got[1], sv.run_ops(n, ops, np.complex128))
     assert np.array_equal(got[0], got[1])
     assert nat.tensor_stage_status() == 0
+
+
+def test_tensor_stage_no_norm_drift_over_many_blocks(rt, tensor_mode):
+    """Accumulated accuracy over a deep circuit (22 qubits, 20 layers of U3 +
+    CX matchings: ~80 fused blocks, and a 22-qubit QFT): the tensor core's
+    accumulator rounds toward zero, which without the host-side compensation
+    shrank the norm by ~1.5e-7 per block (fidelity error ~1e-5 here).
+    Reference: the engine's complex128 run (CUDA-core kernels, checked
+    against the oracle by the other tests).  Bounds: fidelity error and
+    |1 - norm| < 3e-6 (the complex64 CUDA-core path gives ~6e-7)."""
+    import torch
+    nat = tensor_mode
+    rng = np.random.default_rng(22)
+    n = 22
+    qft = []
+    for q in range(n):
+        if rng.random() < 0.5:
+            qft.append(('g', 'X', (), False, q, ()))
+    for i in range(n):
+        qft.append(('g', 'H', (), False, i, ()))
+        for j in range(i + 1, n):
+            qft.append(('g', 'U1', (np.pi / (1 << (j - i)),), False, i, (j,)))
+    for ops in (_u3_cx(rng, n, 20), qft):
+        qs = new_state(rt, n, np.float64)
+        apply_ops(qs, ops)
+        ref = qs.get_raw()
+        qs.delete()
+        qs = new_state(rt, n, np.float32)
+        apply_ops(qs, ops)
+        got = qs.get_raw().astype(np.complex128)
+        norm = qs.processor.calc_norm(qs)
+        qs.delete()
+        ferr = abs(1. - abs(torch.vdot(torch.from_numpy(ref), torch.from_numpy(got)).item()))
+        assert ferr < 3e-6 and abs(1. - norm) < 3e-6, (ferr, norm)
+    assert nat.timing_read('tstage')[0] > 0
+    assert nat.tensor_stage_status() == 0
