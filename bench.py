@@ -146,6 +146,37 @@ def stage_traffic_per_launch(n, cs, kernel_class='stage'):
 
 # ------------------------------------------------------------------ CPU legs
 
+def state_accuracy(rt, qs, gts, n, torch):
+    """Fidelity error |1 - |<psi128|psi64>||, max |p64 - p128| and the
+    complex64 norm of the benchmark circuit's final state (`qs`, complex64)
+    against the same circuit run in complex128 by the engine (CUDA-core
+    FP64 kernels).  Both states are copied to the host; the overlap is summed
+    in FP64 in slices."""
+    qd = rt.create_qubit_states(np.float64)
+    pd = qd.processor
+    pd.initialize_qubit_states(qd, n)
+    pd.reset_qubit_states(qd)
+    for gt, t, c in gts:
+        if c:
+            pd.apply_controlled_gate(gt, False, qd, c, t)
+        else:
+            pd.apply_gate(gt, False, qd, t)
+    ref = qd.get_raw()
+    qd.delete()
+    got = qs.get_raw()
+    norm32 = qs.processor.calc_norm(qs)
+    ov = 0j
+    perr = 0.
+    step = 1 << 24
+    for i in range(0, 1 << n, step):
+        a = torch.from_numpy(ref[i:i + step])
+        b = torch.from_numpy(got[i:i + step]).to(torch.complex128)
+        ov += torch.vdot(a, b).item()
+        perr = max(perr, (a.abs() ** 2 - b.abs() ** 2).abs().max().item())
+    return {'reference': 'the same circuit in complex128 (engine, CUDA-core FP64)',
+            'fidelity_err': abs(1. - abs(ov)), 'max_prob_err': perr, 'norm_c64': norm32}
+
+
 def cpu_port_gate_rate(n, ops, cs, budget_s):
     """Times the oracle's C port of the reference CPU runtime on the first
     gates of the circuit until `budget_s` seconds are spent.  Returns
@@ -302,6 +333,12 @@ def run_gb300(args):
                 'traffic': traffic, 'algorithmic_bytes_per_launch': alg,
                 'launches': dom_launches, 'avg_launch_ms': dom_ms / max(1, dom_launches)}
 
+    # accuracy of the timed state (the last step's) against the same circuit
+    # in complex128
+    accuracy = None
+    if rank == 0 and dtype == np.float32 and not args.no_fidelity:
+        accuracy = state_accuracy(rt, qs, gts, n, torch)
+
     # HBM efficiency of single unfused gate passes (the reference's per-gate sweep)
     single = single_gate_passes(nat, proc, qs, gts, n, cs, torch)
 
@@ -354,6 +391,7 @@ def run_gb300(args):
                 'circuit_ms': t_max / args.steps,
                 'gates_per_s': stats['gates'] / args.steps / (t_max / args.steps / 1e3)}),
             'roofline': roofline,
+            'accuracy': accuracy,
             'adjoint': adjoint,
             'batch': batch,
             'large_states': c4,
@@ -593,6 +631,8 @@ def main():
     ap.add_argument('--samples', type=int, default=10_000_000)
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-fidelity', action='store_true',
+                    help='skip the complex64-vs-complex128 accuracy check of the final state')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
