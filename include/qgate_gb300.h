@@ -158,6 +158,15 @@ int qg_set_stage_pipelining(int on);
  * reference applies one gate per pass
  * (qgate/simulator/src/CUDAQubitProcessor.cpp:271, applyGate). */
 int qg_set_tensor_blocks(int on);
+/* Extension: 1 lets the getter kernels (gathered states, probability arrays)
+ * write straight into the caller's host buffers, allowed only when the
+ * device accesses pageable host memory through the host page tables (Grace +
+ * NVLink-C2C); faster into buffers the caller reuses, much slower into fresh
+ * ones (first touch by GPU page faults).  0 (default) stages every transfer
+ * through pinned buffers.  The reference copies through its own pinned buffers
+ * (qgate/simulator/src/DeviceGetStates.cu:115-119,
+ * qgate/simulator/src/CUDADevice.cpp:37). */
+int qg_set_host_direct(int on);
 /* Extension: status word of the tensor-core stage kernels after a
  * synchronize: 0 = every bounded wait completed; nonzero = a wait gave up
  * (that stage's tiles were left unchanged).  reset != 0 clears it. */

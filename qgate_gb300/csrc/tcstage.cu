@@ -476,7 +476,7 @@ void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool 
         kern<<<(unsigned)ctas, threads, smem, stream>>>((float2 *)state, d, tiles);
     };
     if (d.m == 12 && two_per_row)
-        launch(k_tstage<1, 4, 2>, 4, 1024);
+        launch(k_tstage<1, 3, 2>, 3, 768);
     else if (d.m == 12)
         launch(k_tstage<1, 4, 1>, 4, 512);
     else

@@ -155,3 +155,39 @@ def test_sampling_pool_rejects_unnormalised_state(rt):
     lt = _lane_trans([qs], [list(range(4))])
     with pytest.raises(RuntimeError, match='beyond 0.05'):
         getter.create_sampling_pool(list(range(4)), 4, 0, lt, [])
+
+
+def test_direct_host_writes_match_staged(rt):
+    """Getter outputs written by the kernels straight into the caller's
+    pageable buffers (opt-in where the device supports it) equal the
+    pinned-staging path bit for bit: probability vector and gathered states
+    with lane permutation."""
+    from qgate_gb300 import _native as nat
+    info = nat.device_info()
+    if not (info['pageable_memory_access'] and info['pageable_uses_host_page_tables']):
+        pytest.skip('device does not access pageable host memory')
+    rng = np.random.default_rng(5)
+    n = 20
+    ops = random_ops(rng, n, 40, max_controls=2)
+    out = {}
+    try:
+        for direct in (1, 0):
+            nat.call('qg_set_host_direct', direct)
+            for dtype in (np.float32, np.float64):
+                qs = new_state(rt, n, dtype)
+                apply_ops(qs, ops)
+                getter = rt.create_qubits_states_getter(dtype)
+                probs = np.empty(1 << n, dtype)
+                getter.get_states(probs, 0, abs2, [(qs, [Lane(l, (l * 7) % n) for l in range(n)])],
+                                  [], 1 << n, 0, 1)
+                cdt = np.complex64 if dtype == np.float32 else np.complex128
+                amps = np.empty(1 << 12, cdt)
+                getter.get_states(amps, 0, null, [(qs, [Lane(l, l) for l in range(n)])], [],
+                                  1 << 12, 5, 3)
+                out[(direct, dtype)] = (probs, amps)
+                qs.delete()
+    finally:
+        nat.call('qg_set_host_direct', 0)
+    for dtype in (np.float32, np.float64):
+        for a, b in zip(out[(1, dtype)], out[(0, dtype)]):
+            assert np.array_equal(a, b)
