@@ -35,6 +35,7 @@ import json
 import math
 import os
 import statistics
+import platform
 import subprocess
 import sys
 import threading
@@ -146,6 +147,26 @@ def stage_traffic_per_launch(n, cs, kernel_class='stage'):
 
 # ------------------------------------------------------------------ CPU legs
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU
+    baseline's record."""
+    try:
+        out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith('Model name:'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open('/proc/cpuinfo') as f:
+            for line in f:
+                if line.startswith('model name'):
+                    return line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def state_accuracy(rt, qs, gts, n, torch):
     """Fidelity error |1 - |<psi128|psi64>||, max |p64 - p128| and the
     complex64 norm of the benchmark circuit's final state (`qs`, complex64)
@@ -228,6 +249,7 @@ def run_reference(args):
         'vs_baseline': None, 'dtype': args.dtype, 'data': 'synthetic',
         'config': config_block(args, None),
         'cpu_baseline': {'value': value, 'unit': 'GB/s', 'cores': cpu_port.num_threads(),
+                         'cpu_model': cpu_model(),
                          'kind': 'port', 'sample': sample_desc},
         'e2e': {'value': value, 'unit': 'GB/s', 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': 0},
@@ -366,7 +388,7 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         gbs, done, dt, thr = cpu_port_gate_rate(n, ops, cs, args.cpu_seconds)
-        cpu = {'value': gbs, 'unit': 'GB/s', 'cores': thr, 'kind': 'port',
+        cpu = {'value': gbs, 'unit': 'GB/s', 'cores': thr, 'kind': 'port', 'cpu_model': cpu_model(),
                'sample': 'first %d gates of the circuit on a 2^%d %s state in host memory, '
                          '%.1f s' % (done, n, args.dtype, dt)}
 
