@@ -15,17 +15,21 @@
 // into two FP16 parts rounded to nearest, Ah = f16(A), Al = f16(A - Ah),
 // so |A - Ah - Al| <= 2^-24 |A| + 2^-25 (subnormal spacing), the same for B,
 // and D = Ah Bh + Ah Bl + Al Bh in FP32 (the dropped Al Bl term is <= 2^-24
-// relative): about FP32 accuracy per block.
+// relative): about FP32 accuracy per block.  The accumulator rounds toward
+// zero at every MMA, so the correction products are issued first and the
+// four main-product K-steps last, and the host scales each block's rows by
+// the expected shrink of those roundings (tc_compensate).
 //
 // Data path per block: thread r holds row r of the previous layout in
-// registers (64 floats); it splits each amplitude and stores Ah/Al straight
+// registers (64 floats; 32 with two threads per row); it splits each
+// amplitude and stores Ah/Al straight
 // into the block's canonical 128-byte-swizzled K-major operand layout (B:
 // no swizzle, written on the host) - the map from
 // (row, register) to operand slot is GF(2)-linear, so it is a precomputed
 // slot table (SetSlots), and no separate transpose pass exists.  One thread
 // issues the 12 MMAs per 128 rows and commits them to an mbarrier; every
 // thread then reads its row of D back from tensor memory (tcgen05.ld
-// 32x32b.x64), which is the next block's source layout.  The blocks' B
+// 32x32b), which is the next block's source layout.  The blocks' B
 // operands (Bh, Bl: 16 KB per block) arrive once per CTA by bulk async
 // copies (cp.async.bulk) and stay in shared memory.
 //
@@ -44,8 +48,6 @@ __device__ unsigned g_tc_status;
 
 namespace {
 
-using rs::Swz;
-using rs::reg_slot;
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return (unsigned)__cvta_generic_to_shared(p);
