@@ -1022,10 +1022,10 @@ static int stage_take(const std::vector<const PendingGate *> &gates, unsigned lo
 // stages of 12 lanes instead of 47 (and fewer fused blocks per gate), i.e.
 // 30 % fewer passes over the state.
 static void flush_lookahead(Device &d, States *s, std::vector<const PendingGate *> &remaining,
-                            unsigned long long base, int M) {
+                            unsigned long long base, int M, int max_stages = 1 << 30) {
     const int n = s->n_lanes;
     const size_t kWindow = 512;
-    while (!remaining.empty()) {
+    for (int done = 0; !remaining.empty() && done < max_stages; ++done) {
         const unsigned long long q0 = gate_qmask(*remaining[0]);
         if (__builtin_popcountll(q0 | base) > M) {
             run_single_gate(d, s, *remaining[0]);
@@ -1113,6 +1113,37 @@ static void flush_lookahead(Device &d, States *s, std::vector<const PendingGate 
         }
         remaining.swap(deferred);
     }
+}
+
+// Whether a states object's pending gates go to the lookahead planner of
+// tensor-core stages, and its tile size M and always-present lanes `base`.
+static bool lookahead_params(const Device &d, const States *s, int &M, unsigned long long &base) {
+    const int n = s->n_lanes;
+    M = std::min(d.tile_lanes[s->prec], kMaxTileLanes);
+    if (!(d.tensor_blocks && s->prec == kFP32 && (M == 12 || M == 13) && n > M)) return false;
+    base = (1ULL << std::min(n, 4)) - 1;
+    return true;
+}
+
+// Streaming flush: once a states object holds kStreamAt pending gates, the
+// first stage is planned and launched right away (the planner looks 512
+// gates ahead, so it decides as a full flush would), so the GPU works while
+// the caller is still enqueueing the rest of the circuit.
+constexpr size_t kStreamAt = 640;
+
+static void stream_flush(States *s) {
+    Device &d = dev();
+    int M;
+    unsigned long long base;
+    if (s->pending.size() < kStreamAt || !lookahead_params(d, s, M, base)) return;
+    merge_runs(s->pending);
+    std::vector<const PendingGate *> remaining;
+    for (auto &g : s->pending) remaining.push_back(&g);
+    flush_lookahead(d, s, remaining, base, M, 1);
+    std::vector<PendingGate> rest;
+    rest.reserve(remaining.size());
+    for (auto *g : remaining) rest.push_back(*g);
+    s->pending.swap(rest);
 }
 
 // Fusion planner.  Walks the pending gates in order and packs them into
@@ -1664,6 +1695,7 @@ static void enqueue_gate(qg_handle hp, const double *mat, qg_handle hs, const in
     g.diag = is_diag(g.m);
     s->pending.push_back(g);
     g_dev.n_gates += 1;
+    stream_flush(s);
 }
 
 int qg_qubit_processor_apply_gate(qg_handle hp, const double *mat, qg_handle hs, int lane) {
