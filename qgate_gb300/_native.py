@@ -47,8 +47,9 @@ SIGNATURES = {
     'qg_qubit_processor_decohere': [_h, _i, _d, _h, _i],
     'qg_qubit_processor_decohere_and_separate': [_h, _i, _d, _h, _h, _h, _i],
     'qg_qubit_processor_apply_reset': [_h, _h, _i],
-    'qg_qubit_processor_apply_gate': [_h, _dp, _h, _i],
-    'qg_qubit_processor_apply_controlled_gate': [_h, _dp, _h, _ip, _i, _i],
+    # per-gate entry points take raw addresses (ints) for speed
+    'qg_qubit_processor_apply_gate': [_h, _vp, _h, _i],
+    'qg_qubit_processor_apply_controlled_gate': [_h, _vp, _h, _vp, _i, _i],
     'qg_qubit_processor_apply_multi': [_h, _dp, _h, _ip, _i, _ip, _i],
     'qg_qubit_processor_calc_pauli_expectation': [_h, _h, _u64, _u64, _dp],
     'qg_qubit_processor_calc_norm': [_h, _h, _dp],
@@ -65,7 +66,7 @@ SIGNATURES = {
     'qg_device_info': [_i64p, _i],
     'qg_qubit_states_get_raw': [_h, _vp, _i64],
     'qg_qubit_states_set_raw': [_h, _vp, _i64],
-    'qg_gate_matrix': [ctypes.c_char_p, _dp, _i, _i, _dp],
+    'qg_gate_matrix': [ctypes.c_char_p, _vp, _i, _i, _vp],
     'qg_calc_probability_noalloc': [_i, _vp, _i, _i, _vp, _u64],
     'qg_adjoint_expectation': [_i, _i, _vp, _i, _vp, _i, _i, _vp, _i, _i, _vp, _vp],
     'qg_batch_sum_z': [_i, _i, _vp, _vp, _vp, _vp],
@@ -141,8 +142,8 @@ def gate_matrix(name, args=(), adjoint=False):
     qgate/simulator/src/GateMatrix.cpp:13-158)."""
     a = np.ascontiguousarray(np.asarray(args, dtype=np.float64).reshape(-1))
     out = np.empty(8, np.float64)
-    check(lib.qg_gate_matrix(name.encode(), as_dptr(a) if a.size else None, int(a.size),
-                             1 if adjoint else 0, as_dptr(out)))
+    check(lib.qg_gate_matrix(name.encode(), a.ctypes.data if a.size else None, int(a.size),
+                             1 if adjoint else 0, out.ctypes.data))
     return out.view(np.complex128).reshape(2, 2)
 
 

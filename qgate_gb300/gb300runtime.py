@@ -82,6 +82,32 @@ atexit.register(module_finalize)
 # ---------------------------------------------------------------- gate matrices
 
 _matrix_cache = {}
+_name_bytes = {}
+_ctrl_cache = {}
+_gate_matrix_fn = nat.lib.qg_gate_matrix
+_apply_gate_fn = nat.lib.qg_qubit_processor_apply_gate
+_apply_controlled_fn = nat.lib.qg_qubit_processor_apply_controlled_gate
+
+
+def _matrix_entry(gate_type, adjoint):
+    """(matrix, its address): the 2x2 complex128 matrix of a gate type as 8
+    contiguous doubles, cached per (class, args, adjoint)."""
+    cls = type(gate_type)
+    args = getattr(gate_type, 'args', ())
+    key = (cls, tuple(args), bool(adjoint))
+    e = _matrix_cache.get(key)
+    if e is None:
+        name = _name_bytes.get(cls)
+        if name is None:
+            name = _name_bytes.setdefault(cls, cls.__name__.encode())
+        a = np.asarray(args, np.float64).reshape(-1)
+        m = np.empty(8, np.float64)
+        nat.check(_gate_matrix_fn(name, a.ctypes.data if a.size else None, a.size,
+                                  1 if adjoint else 0, m.ctypes.data))
+        if len(_matrix_cache) > 4096:
+            _matrix_cache.clear()
+        e = _matrix_cache[key] = (m, m.ctypes.data)
+    return e
 
 
 def gate_matrix(gate_type, adjoint):
@@ -90,16 +116,19 @@ def gate_matrix(gate_type, adjoint):
     The reference builds it from the `cmatf` factory registered per gate
     class (qgate/simulator/cpumatrix.py:4-20, qgate/simulator/src/glue.cpp:383-395);
     here the class name and `args` select the same formulas in the C ABI."""
-    name = type(gate_type).__name__
-    args = tuple(float(a) for a in getattr(gate_type, 'args', ()))
-    key = (name, args, bool(adjoint))
-    m = _matrix_cache.get(key)
-    if m is None:
-        m = np.ascontiguousarray(nat.gate_matrix(name, args, adjoint).reshape(-1)).view(np.float64)
-        if len(_matrix_cache) > 4096:
-            _matrix_cache.clear()
-        _matrix_cache[key] = m
-    return m
+    return _matrix_entry(gate_type, adjoint)[0]
+
+
+def _controls(lanes):
+    """(int32 array, address) of a control-lane list, cached per tuple."""
+    key = tuple(lanes)
+    e = _ctrl_cache.get(key)
+    if e is None:
+        a = nat.int_array(key)
+        if len(_ctrl_cache) > 4096:
+            _ctrl_cache.clear()
+        e = _ctrl_cache[key] = (a, a.ctypes.data)
+    return e
 
 
 # ---------------------------------------------------------------- processor / states
@@ -156,16 +185,18 @@ class GB300QubitProcessor:
         nat.call('qg_qubit_processor_apply_reset', self.ptr, qstates.ptr, int(local_lane))
 
     def apply_gate(self, gate_type, _adjoint, qstates, local_lane):
-        m = gate_matrix(gate_type, _adjoint)
-        nat.call('qg_qubit_processor_apply_gate', self.ptr, nat.as_dptr(m), qstates.ptr,
-                 int(local_lane))
+        st = _apply_gate_fn(self.ptr, _matrix_entry(gate_type, _adjoint)[1], qstates.ptr,
+                            int(local_lane))
+        if st:
+            nat.check(st)
 
     def apply_controlled_gate(self, gate_type, _adjoint, qstates, local_control_lanes,
                               local_target_lane):
-        m = gate_matrix(gate_type, _adjoint)
-        ctrl = nat.int_array(local_control_lanes)
-        nat.call('qg_qubit_processor_apply_controlled_gate', self.ptr, nat.as_dptr(m),
-                 qstates.ptr, nat.as_iptr(ctrl), len(ctrl), int(local_target_lane))
+        ctrl, addr = _controls(local_control_lanes)
+        st = _apply_controlled_fn(self.ptr, _matrix_entry(gate_type, _adjoint)[1], qstates.ptr,
+                                  addr, len(ctrl), int(local_target_lane))
+        if st:
+            nat.check(st)
 
     # ---- extensions (no counterpart in the reference runtime protocol)
 
