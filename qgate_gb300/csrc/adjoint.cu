@@ -324,6 +324,14 @@ void adj_dispatch(void *psi, void *lam, const AdjStageDesc &d, const void *mats,
     switch (d.rl) {
     case 3: launch(k_adj_stage<R, 3, MODE>); break;
     case 4: launch(k_adj_stage<R, 4, MODE>); break;
+    case 5:
+        // forward stages of complex64 only (the backward holds psi and
+        // lambda: 2 x 32 amplitudes per thread would not fit)
+        if constexpr (MODE == 0 && sizeof(R) == 4)
+            launch(k_adj_stage<R, 5, MODE>);
+        else
+            fail(2, "adjoint stage: 5 register lanes only for complex64 forward stages");
+        break;
     default: fail(2, "adjoint stage: unsupported register lanes %d", d.rl);
     }
     QG_CUDA(cudaGetLastError());

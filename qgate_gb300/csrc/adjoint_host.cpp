@@ -327,6 +327,9 @@ static void adjoint_run(int prec, int n, std::vector<Op> &ops, const double *par
     const size_t cs = sizeof(R) * 2;
     const size_t state_bytes = cs << n;
     const int rl = n >= 9 ? 4 : 3;
+    // complex64 forward stages keep 32 amplitudes per thread (256 threads
+    // per 13-lane tile); everything else 16 (or 8 on small states)
+    const int rl_fwd = (sizeof(R) == 4 && n >= 13) ? 5 : rl;
     const int M_fwd = std::min(n, rl == 4 ? 13 : 12);
     const int M_bwd = std::min(n, rl == 4 ? 12 : 11);
     const int budget = 0;
@@ -347,7 +350,7 @@ static void adjoint_run(int prec, int n, std::vector<Op> &ops, const double *par
         std::vector<int> order;
         for (int j = bounds[s]; j < bounds[s + 1]; ++j) order.push_back(j);
         size_t first = launches.size();
-        build_launches<R>(ops, order, n, M_fwd, rl, budget, 0, batch, n_params, params, launches,
+        build_launches<R>(ops, order, n, M_fwd, rl_fwd, budget, 0, batch, n_params, params, launches,
                           mats, slot_param, slot_scale);
         if (s + 1 < nseg && launches.size() > first) launches.back().ckpt_after = s;
         if (s + 1 < nseg && launches.size() == first) fail(QG_ERR_VALUE, "empty segment.");
