@@ -167,6 +167,11 @@ int qg_set_tensor_blocks(int on);
  * (qgate/simulator/src/DeviceGetStates.cu:115-119,
  * qgate/simulator/src/CUDADevice.cpp:37). */
 int qg_set_host_direct(int on);
+/* Extension: 1 (default where the device accesses pageable host memory)
+ * returns large results (64 MiB .. 16 GiB) through one device buffer and one
+ * copy into the caller's buffer, after touching its pages with all host
+ * threads; 0 stages them through pinned buffers in 64 MiB pieces. */
+int qg_set_pageable_copy(int on);
 /* Extension: status word of the tensor-core stage kernels after a
  * synchronize: 0 = every bounded wait completed; nonzero = a wait gave up
  * (that stage's tiles were left unchanged).  reset != 0 clears it. */

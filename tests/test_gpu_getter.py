@@ -191,3 +191,37 @@ def test_direct_host_writes_match_staged(rt):
     for dtype in (np.float32, np.float64):
         for a, b in zip(out[(1, dtype)], out[(0, dtype)]):
             assert np.array_equal(a, b)
+
+
+def test_pageable_copy_matches_staged(rt):
+    """Large getter results (>= 64 MiB) go through one device buffer and one
+    copy into the caller's pageable array where the device supports it (the
+    default there); they equal the pinned-staging path bit for bit: a 24-qubit
+    complex64 probability vector (64 MiB) and the state itself (128 MiB),
+    into fresh and reused arrays."""
+    from qgate_gb300 import _native as nat
+    info = nat.device_info()
+    if not (info['pageable_memory_access'] and info['pageable_uses_host_page_tables']):
+        pytest.skip('device does not access pageable host memory')
+    rng = np.random.default_rng(24)
+    n = 24
+    ops = random_ops(rng, n, 30, max_controls=1)
+    qs = new_state(rt, n, np.float32)
+    apply_ops(qs, ops)
+    getter = rt.create_qubits_states_getter(np.float32)
+    lanes = [(qs, [Lane(l, l) for l in range(n)])]
+    out = {}
+    try:
+        for pc in (1, 0):
+            nat.call('qg_set_pageable_copy', pc)
+            probs = np.empty(1 << n, np.float32)
+            getter.get_states(probs, 0, abs2, lanes, [], 1 << n, 0, 1)
+            again = probs.copy()
+            getter.get_states(again, 0, abs2, lanes, [], 1 << n, 0, 1)
+            out[pc] = (probs, again, qs.get_raw())
+    finally:
+        nat.call('qg_set_pageable_copy', 1)
+    for a, b in zip(out[1], out[0]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(out[1][0], out[1][1])
+    qs.delete()
