@@ -2376,6 +2376,37 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
         return QG_OK;
     }
     Device &d = dev();
+    const size_t bytes = (size_t)n_samples * 8;
+    if (d.pageable_copy && bytes >= ((size_t)64 << 20) && bytes <= ((size_t)8 << 30)) {
+        // One copy each way between the caller's pageable arrays and device
+        // buffers (Grace + NVLink-C2C); the index array's pages are touched
+        // by all host threads while the uniforms go up and the search runs.
+        double *du = (double *)d.arena.alloc(bytes);
+        long long *dobs = (long long *)d.arena.alloc(bytes);
+        try {
+            QG_CUDA(cudaMemcpyAsync(du, randnum, bytes, cudaMemcpyHostToDevice, d.stream));
+            timed(d, "search", [&] {
+                launch_search(p->cdf, p->n, du, dobs, n_samples, p->empty_pos.data(),
+                              (int)p->empty_pos.size(), d.stream);
+            });
+            char *h = (char *)obs;
+            const size_t kPage = 4096;
+#pragma omp parallel for schedule(static)
+            for (long long i = 0; i < (long long)((bytes + kPage - 1) / kPage); ++i)
+                ((volatile char *)h)[(size_t)i * kPage] = 0;
+            QG_CUDA(cudaMemcpyAsync(obs, dobs, bytes, cudaMemcpyDeviceToHost, d.stream));
+            QG_CUDA(cudaStreamSynchronize(d.stream));
+        } catch (...) {
+            cudaStreamSynchronize(d.stream);
+            d.arena.release(du);
+            d.arena.release(dobs);
+            throw;
+        }
+        d.arena.release(du);
+        d.arena.release(dobs);
+        t_last_error.clear();
+        return QG_OK;
+    }
     // Uniforms go up through staging buffer 0, indices come back through 1.
     idx_t chunk = (idx_t)(Device::kStageBytes / 8);
     double *du = (double *)d.arena.alloc(chunk * 8);
