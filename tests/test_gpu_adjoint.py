@@ -152,3 +152,20 @@ def test_torch_autograd_function():
     for b in range(4):
         g = ao.parameter_shift(n, c.ops, thetas.detach().numpy()[b], H.terms)
         assert np.max(np.abs(thetas.grad.numpy()[b] - g)) < 1e-10
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_adjoint_matches_reference_parameter_shift(dtype):
+    """The engine's adjoint gradients of the 12-qubit, 12-layer
+    hardware-efficient ansatz (288 parameters) against the parameter-shift
+    gradients the reference computed on its own C++ CPU runtime in complex128
+    (tests/golden/gradients_hea12.npz).  complex128 1e-10, complex64 1e-5."""
+    import os
+    from qgate_gb300.adjoint import expectation_and_gradient, hardware_efficient_ansatz, PauliSum
+    g = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'gradients_hea12.npz'))
+    n = 12
+    c = hardware_efficient_ansatz(n, 12)
+    H = PauliSum.ising_chain(n)
+    E, G = expectation_and_gradient(c, g['params'], H, dtype, checkpoint_every=3 * 3 * n)
+    assert abs(E[0] - float(g['energy'])) < TOL[dtype]
+    assert np.max(np.abs(G[0] - g['grad'])) < TOL[dtype], np.max(np.abs(G[0] - g['grad']))

@@ -75,3 +75,22 @@ def test_u3_decomposition_matches_reference_matrix():
             sv.apply_gate(psi, ao.rotation_matrix(axis, coef * th[p]), target)
         U[:, col] = psi
     assert np.allclose(U, sv.gate_matrix('U', tuple(th)), atol=1e-14)
+
+
+def test_oracle_gradients_match_reference_parameter_shift():
+    """The oracle's energy and parameter-shift gradients of the 12-qubit,
+    12-layer hardware-efficient ansatz (Ry, Rz + CX ring; transverse-field
+    Ising chain) equal the ones the reference computed on its own C++ CPU
+    runtime in complex128 (tests/golden/gradients_hea12.npz, written by
+    tests/golden/make_gradients.py)."""
+    import os
+    from qgate_gb300.adjoint import PauliSum, hardware_efficient_ansatz
+    g = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'gradients_hea12.npz'))
+    n = 12
+    c = hardware_efficient_ansatz(n, 12)
+    H = PauliSum.ising_chain(n)
+    params = g['params']
+    assert c.n_params == len(params)
+    assert abs(ao.energy(n, c.ops, params, H.terms) - float(g['energy'])) < 1e-10
+    ps = ao.parameter_shift(n, c.ops, params, H.terms)
+    assert np.max(np.abs(ps - g['grad'])) < 1e-10
