@@ -13,6 +13,7 @@
 // (qgate/simulator/src/GateMatrix.cpp:114-141); U3 is Rz(phi) Ry(theta)
 // Rz(lambda) (GateMatrix.cpp:14-25) and is decomposed by the caller.
 #include "qg_internal.h"
+#include "qg_plan.h"
 #include "../../include/qgate_gb300.h"
 
 #include <algorithm>
@@ -316,6 +317,92 @@ void build_launches(const std::vector<Op> &ops, const std::vector<int> &order, i
     }
 }
 
+// Forward sweep on the tensor cores (complex64 states of >= 13 qubits, when
+// tensor-core stages are on).  The stages of each checkpoint segment are
+// planned like the gate queue's (plan_stage_lanes over 12-lane tiles); the
+// lanes, blocks and layouts depend only on the gates' lanes, so they are the
+// same for every parameter vector, and only the block unitaries differ: one
+// k_tstage launch per stage and vector, each with that vector's operands.
+struct TcForward {
+    struct Step {
+        TcStageDesc desc;     // bmats filled at launch
+        size_t ops_off;       // FP16 offset of batch element 0's operands
+        size_t ops_stride;    // FP16 per batch element
+        int ckpt_after;       // save psi to this checkpoint after the step (-1: none)
+    };
+    std::vector<Step> steps;
+    std::vector<unsigned short> ops;  // [step][batch][nb][Bh | Bl]
+};
+
+void plan_tc_forward(const std::vector<Op> &ops, const std::vector<int> &bounds, int n, int batch,
+                     int n_params, const double *params, TcForward &out) {
+    const int M = 12;
+    const unsigned long long base = (1ULL << 4) - 1;
+    const size_t kBlockHalves = 2 * 64 * 64;
+    const int per_launch = tstage_max_blocks(M);
+    auto gate_of = [&](const Op &o, int b) {
+        PendingGate g;
+        g.target = o.target;
+        g.controls = o.controls;
+        if (o.kind == 1)
+            rotation(o.axis, o.coef * params[(size_t)b * n_params + o.param], g.m.v);
+        else
+            memcpy(g.m.v, o.mat, sizeof(g.m.v));
+        g.diag = is_diag(g.m);
+        return g;
+    };
+    const int nseg = (int)bounds.size() - 1;
+    for (int sgi = 0; sgi < nseg; ++sgi) {
+        // planning on batch element 0's gates (only their lanes matter)
+        std::vector<PendingGate> g0;
+        for (int j = bounds[sgi]; j < bounds[sgi + 1]; ++j) g0.push_back(gate_of(ops[j], 0));
+        std::vector<const PendingGate *> remaining;
+        for (auto &g : g0) remaining.push_back(&g);
+        while (!remaining.empty()) {
+            unsigned long long S = plan_stage_lanes(remaining, base, M);
+            std::vector<const PendingGate *> chosen, deferred;
+            stage_take(remaining, S, remaining.size(), &chosen, &deferred);
+            for (int q = 0; q < n && __builtin_popcountll(S) < M; ++q) S |= 1ULL << q;
+            const TileLanes tl = tile_lanes_of(S, n);
+            const TcBlocks blocks0 = tc_blocks(chosen, tl);
+            // the blocks as indices into the segment's gates
+            std::vector<std::pair<unsigned, std::vector<int>>> bidx;
+            for (auto &bl : blocks0) {
+                std::vector<int> ix;
+                for (auto *g : bl.second) ix.push_back((int)(g - g0.data()));
+                bidx.emplace_back(bl.first, ix);
+            }
+            for (size_t b0 = 0; b0 < bidx.size(); b0 += per_launch) {
+                const int nb = (int)std::min<size_t>(per_launch, bidx.size() - b0);
+                TcForward::Step st;
+                st.ops_off = out.ops.size();
+                st.ops_stride = nb * kBlockHalves;
+                st.ckpt_after = -1;
+                out.ops.resize(out.ops.size() + (size_t)batch * st.ops_stride);
+                std::vector<TcStageDesc> descs(batch);
+#pragma omp parallel for schedule(dynamic, 1)
+                for (int b = 0; b < batch; ++b) {
+                    std::vector<PendingGate> gb;
+                    gb.reserve(g0.size());
+                    for (int j = bounds[sgi]; j < bounds[sgi + 1]; ++j) gb.push_back(gate_of(ops[j], b));
+                    TcBlocks blocks;
+                    for (auto &bi : bidx) {
+                        std::vector<const PendingGate *> ptrs;
+                        for (int ix : bi.second) ptrs.push_back(&gb[ix]);
+                        blocks.emplace_back(bi.first, ptrs);
+                    }
+                    tc_plan_launch(tl, n, blocks, b0, nb, descs[b],
+                                   out.ops.data() + st.ops_off + (size_t)b * st.ops_stride);
+                }
+                st.desc = descs[0];
+                out.steps.push_back(st);
+            }
+            remaining.swap(deferred);
+        }
+        if (sgi + 1 < nseg && !out.steps.empty()) out.steps.back().ckpt_after = sgi;
+    }
+}
+
 }  // namespace
 
 template <class R>
@@ -346,14 +433,21 @@ static void adjoint_run(int prec, int n, std::vector<Op> &ops, const double *par
     std::vector<R> mats;
     std::vector<int> slot_param;
     std::vector<double> slot_scale;
-    for (int s = 0; s < nseg; ++s) {
-        std::vector<int> order;
-        for (int j = bounds[s]; j < bounds[s + 1]; ++j) order.push_back(j);
-        size_t first = launches.size();
-        build_launches<R>(ops, order, n, M_fwd, rl_fwd, budget, 0, batch, n_params, params, launches,
-                          mats, slot_param, slot_scale);
-        if (s + 1 < nseg && launches.size() > first) launches.back().ckpt_after = s;
-        if (s + 1 < nseg && launches.size() == first) fail(QG_ERR_VALUE, "empty segment.");
+    // complex64 forward sweeps of >= 13 qubits run on the tensor cores
+    const bool tc_fwd = sizeof(R) == 4 && n >= 13 && tensor_stages_enabled();
+    TcForward tcf;
+    if (tc_fwd) {
+        plan_tc_forward(ops, bounds, n, batch, n_params, params, tcf);
+    } else {
+        for (int s = 0; s < nseg; ++s) {
+            std::vector<int> order;
+            for (int j = bounds[s]; j < bounds[s + 1]; ++j) order.push_back(j);
+            size_t first = launches.size();
+            build_launches<R>(ops, order, n, M_fwd, rl_fwd, budget, 0, batch, n_params, params,
+                              launches, mats, slot_param, slot_scale);
+            if (s + 1 < nseg && launches.size() > first) launches.back().ckpt_after = s;
+            if (s + 1 < nseg && launches.size() == first) fail(QG_ERR_VALUE, "empty segment.");
+        }
     }
     const size_t n_fwd = launches.size();
     if (G_out) {
@@ -406,6 +500,24 @@ static void adjoint_run(int prec, int n, std::vector<Op> &ops, const double *par
         // |0...0> for every batch element
         for (int b = 0; b < batch; ++b)
             launch_init_basis(prec, (char *)psi + state_bytes * b, (idx_t)1 << n, st);
+
+        if (tc_fwd) {
+            unsigned short *dops = (unsigned short *)alloc(
+                std::max<size_t>(tcf.ops.size() * sizeof(unsigned short), 16));
+            QG_CUDA(cudaMemcpyAsync(dops, tcf.ops.data(), tcf.ops.size() * sizeof(unsigned short),
+                                    cudaMemcpyHostToDevice, st));
+            for (auto &step : tcf.steps) {
+                TcStageDesc d = step.desc;
+                for (int b = 0; b < batch; ++b) {
+                    d.bmats = dops + step.ops_off + (size_t)b * step.ops_stride;
+                    launch_tstage((char *)psi + state_bytes * b, d, st, false);
+                }
+                if (step.ckpt_after >= 0 && ck)
+                    QG_CUDA(cudaMemcpyAsync((char *)ck + state_bytes * batch * step.ckpt_after,
+                                            psi, state_bytes * batch, cudaMemcpyDeviceToDevice,
+                                            st));
+            }
+        }
 
         for (size_t li = 0; li < launches.size(); ++li) {
             Launch &L = launches[li];

@@ -10,6 +10,7 @@
 // (qgate/simulator/src/CUDAQubitProcessor.cpp:40-50,
 // qgate/simulator/src/DeviceSum.h:16-23).
 #include "qg_internal.h"
+#include "qg_plan.h"
 #include "../../include/qgate_gb300.h"
 
 #include <algorithm>
@@ -110,13 +111,6 @@ struct Arena {
 };
 
 // ------------------------------------------------------------ objects
-
-struct PendingGate {
-    int target;
-    std::vector<int> controls;
-    Mat2 m;
-    bool diag;
-};
 
 struct States {
     int prec;
@@ -228,6 +222,7 @@ static Device &dev() {
 
 cudaStream_t engine_stream() { return dev().stream; }
 void *engine_alloc(size_t bytes) { return dev().arena.alloc(bytes); }
+bool tensor_stages_enabled() { return dev().tensor_blocks; }
 void engine_free(void *p) { g_dev.arena.release(p); }
 
 template <class T> static T *lookup(std::unordered_set<T *> &set, qg_handle h, const char *what) {
@@ -314,33 +309,6 @@ static void run_single_gate(Device &d, States *s, const PendingGate &g) {
     timed(d, "gate", [&] { launch_apply_pairs(s->prec, s->d, n_items, pi, g.m, d.stream); });
     d.n_passes += 1;
     d.n_bytes += 4 * n_items * (long long)complex_size(s->prec);
-}
-
-static unsigned long long gate_qmask(const PendingGate &g) {
-    unsigned long long q = 1ULL << g.target;
-    for (int c : g.controls) q |= 1ULL << c;
-    return q;
-}
-
-static bool is_diag(const Mat2 &m) {
-    return m.v[2] == 0. && m.v[3] == 0. && m.v[4] == 0. && m.v[5] == 0.;
-}
-
-struct TileLanes {
-    std::vector<int> lanes;  // global lanes of the tile, ascending
-    int local_of[64];
-    int lowrun;
-};
-
-static TileLanes tile_lanes_of(unsigned long long S, int n) {
-    TileLanes tl;
-    for (int q = 0; q < n; ++q)
-        if (S & (1ULL << q)) tl.lanes.push_back(q);
-    for (int i = 0; i < 64; ++i) tl.local_of[i] = -1;
-    for (int i = 0; i < (int)tl.lanes.size(); ++i) tl.local_of[tl.lanes[i]] = i;
-    tl.lowrun = 0;
-    while (tl.lowrun < (int)tl.lanes.size() && tl.lanes[tl.lowrun] == tl.lowrun) ++tl.lowrun;
-    return tl;
 }
 
 // Shared-memory stage (generic, any tile size): used for tiles too small for
@@ -512,363 +480,6 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
     return true;
 }
 
-// ------------------------------------------------------------ tensor-core stages
-
-// Register layout of a tile: thread r holds row r (bits i of r at tile
-// positions rows[i]), register pair j holds amplitude j (bits k of j at
-// tile positions amps[k]).
-struct TcLayout {
-    int rows[8];
-    int amps[5];
-};
-
-// Operand layout of a block (tile index -> operand slot; a slot is one
-// complex amplitude as f16x2, 4 bytes): the canonical K-major layout with the
-// 128-byte swizzle.  Before the swizzle, row r of a 128-row group is 128
-// contiguous bytes (its 32 amplitudes: amps[0..4] -> slot bits 0..4), rows
-// r % 8 -> bits 5..7 (128 bytes apart), r / 8 -> bits 8..11 (8-row atoms of
-// 1024 bytes, the stride byte offset), rows[7] -> bit 12 (second 128-row
-// group, 16384 bytes); r's bits are rows[0..6].  The swizzle XORs the 16-byte
-// chunk index (slot bits 2..4) with r % 8 (slot bits 5..7).  All of it is a
-// GF(2)-linear map of the tile index.
-static unsigned tc_operand_slot(const TcLayout &L, unsigned tidx) {
-    unsigned c = 0;
-    for (int k = 0; k < 5; ++k)
-        if (tidx >> L.amps[k] & 1u) c |= 1u << k;
-    for (int i = 0; i < 8; ++i)
-        if (L.rows[i] >= 0 && (tidx >> L.rows[i] & 1u)) c |= 1u << (i < 7 ? 5 + i : 12);
-    return c ^ (((c >> 5) & 7u) << 2);
-}
-
-template <class F> static SetSlots tc_slots(const TcLayout &src, int t, F dst) {
-    SetSlots ss;
-    memset(&ss, 0, sizeof(ss));
-    auto dep = [&](unsigned x) {
-        unsigned ti = 0;
-        for (int i = 0; i < t; ++i)
-            if (x >> i & 1u) ti |= 1u << src.rows[i];
-        return ti;
-    };
-    for (unsigned x = 0; x < 32; ++x) ss.lo[x] = (unsigned short)dst(dep(x));
-    for (unsigned x = 0; x < 16 && (x << 5) < (1u << t); ++x)
-        ss.hi[x] = (unsigned short)dst(dep(x << 5));
-    for (int k = 0; k < 5; ++k) ss.q[k] = (unsigned short)dst(1u << src.amps[k]);
-    return ss;
-}
-
-// IEEE binary16 bits of x, rounded to nearest even (subnormals kept).
-static unsigned short f16_bits(float x) {
-    unsigned f;
-    memcpy(&f, &x, 4);
-    const unsigned sign = (f >> 16) & 0x8000u;
-    const int e = (int)((f >> 23) & 0xffu) - 127 + 15;
-    unsigned mant = f & 0x7fffffu;
-    if (e >= 31) return (unsigned short)(sign | 0x7c00u);
-    if (e <= 0) {
-        if (e < -10) return (unsigned short)sign;
-        mant |= 0x800000u;
-        const int shift = 14 - e;
-        unsigned hm = mant >> shift;
-        const unsigned rem = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
-        if (rem > half || (rem == half && (hm & 1u))) ++hm;
-        return (unsigned short)(sign | hm);
-    }
-    unsigned out = ((unsigned)e << 10) | (mant >> 13);
-    const unsigned rem = mant & 0x1fffu;
-    if (rem > 0x1000u || (rem == 0x1000u && (out & 1u))) ++out;
-    return (unsigned short)(sign | out);
-}
-
-static double f16_value(unsigned short h) {
-    const int e = (h >> 10) & 31, mant = h & 1023;
-    double v = e == 0 ? std::ldexp((double)mant, -24) : std::ldexp((double)(mant | 1024), e - 25);
-    return (h & 0x8000u) ? -v : v;
-}
-
-// Split operand of a 32x32 complex block U (row-major, amplitude order of
-// the block layout): B[k][n] of D = A B with A[r][2i + c] = (Re, Im) V[r][i]
-// and D[r][2o + c] = (Re, Im) (U V[r])[o], stored K-major (row n holds its
-// K elements) in the canonical no-swizzle layout: element (n, k) at FP16
-// index (k / 16) * 1024 + (k % 16 / 8) * 512 + (n / 8) * 64 + (n % 8) * 8 +
-// k % 8.  Bh = f16(B), Bl = f16(B - Bh), both rounded to nearest.
-static void tc_operand(const std::complex<double> *U, unsigned short *bh, unsigned short *bl) {
-    for (int o = 0; o < 32; ++o)
-        for (int i = 0; i < 32; ++i) {
-            const double re = U[o * 32 + i].real(), im = U[o * 32 + i].imag();
-            const double val[2][2] = {{re, -im}, {im, re}};  // [c_out][c_in]
-            for (int co = 0; co < 2; ++co)
-                for (int ci = 0; ci < 2; ++ci) {
-                    const int n = 2 * o + co, k = 2 * i + ci;
-                    const size_t at = (size_t)(k / 16) * 1024 + (k % 16 / 8) * 512 +
-                                      (n / 8) * 64 + (n % 8) * 8 + k % 8;
-                    const double x = val[co][ci];
-                    const unsigned short h = f16_bits((float)x);
-                    bh[at] = h;
-                    bl[at] = f16_bits((float)(x - f16_value(h)));
-                }
-        }
-}
-
-// Bias compensation for the tensor core's accumulator.  The FP32 accumulator
-// of tcgen05.mma rounds toward zero at every MMA, so each output shrinks in
-// magnitude by half an ulp per rounding on average; the kernel orders the
-// MMAs so that only the main product's K-steps round at full magnitude, and
-// an output whose inputs span c of the four K-steps sees roundings at about
-// 1/c, 2/c, ..., 1 of its final value: an expected relative shrink of
-// (c + 1) / 4 * kRzShrink, kRzShrink being the mean relative shrink of one
-// rounding at full magnitude (measured on GB300 from the norm drift of
-// dense blocks: 7.25e-8 per block for c = 4).  Each row of U is scaled up by
-// that amount, which removes the drift (it would otherwise shrink the norm by
-// ~1.5e-7 per block); the remaining error is unbiased.
-constexpr double kRzShrink = 5.8e-8;
-
-static void tc_compensate(std::complex<double> *U) {
-    for (int o = 0; o < 32; ++o) {
-        int c = 0;
-        for (int ks = 0; ks < 4; ++ks) {
-            bool nz = false;
-            for (int i = 8 * ks; i < 8 * ks + 8; ++i) nz |= U[o * 32 + i] != 0.;
-            c += nz;
-        }
-        if (c == 0) continue;
-        const double f = 1. + 0.25 * (c + 1) * kRzShrink;
-        for (int i = 0; i < 32; ++i) U[o * 32 + i] *= f;
-    }
-}
-
-// Greedy 5-lane blocks over a stage's gates in order: a gate joins the open
-// block when its lanes fit and no earlier deferred gate shares a lane (so it
-// commutes with everything deferred); the rest start the next block.
-static std::vector<std::pair<unsigned, std::vector<const PendingGate *>>>
-tc_blocks(const std::vector<const PendingGate *> &gates, const TileLanes &tl) {
-    std::vector<std::pair<unsigned, std::vector<const PendingGate *>>> out;
-    std::vector<const PendingGate *> rem(gates);
-    while (!rem.empty()) {
-        unsigned L = 0, blocked = 0;
-        std::vector<const PendingGate *> take, keep;
-        for (auto *g : rem) {
-            unsigned q = 1u << tl.local_of[g->target];
-            for (int c : g->controls) q |= 1u << tl.local_of[c];
-            if ((q & blocked) || __builtin_popcount(L | q) > 5) {
-                keep.push_back(g);
-                blocked |= q;
-                continue;
-            }
-            L |= q;
-            take.push_back(g);
-        }
-        out.emplace_back(L, std::move(take));
-        rem.swap(keep);
-    }
-    return out;
-}
-
-// Orders a block's lanes and rows so that the stores into its operand hit
-// distinct banks.  The bank of a slot is bits 0..4 of tc_operand_slot:
-// amps[0], amps[1], amps[2] ^ rows[0], amps[3] ^ rows[1], amps[4] ^ rows[2];
-// a warp's threads differ in the source layout's rows[0..4] (W), so the
-// stores are conflict-free when W's lanes drive the five bank bits one each:
-// two W lanes of the block as amps[0..1], further W lanes of the block as
-// amps[2..4], and W's other lanes as the rows[k] whose amps[k + 2] is not a W
-// lane.  That works whenever the block holds at least two W lanes.  rows[3..4]
-// are then chosen so that the next block can do the same (at least two of
-// this layout's rows[0..4] among its lanes).
-static TcLayout tc_choose_layout(unsigned lanes, unsigned next_lanes, const TcLayout &src, int m) {
-    unsigned W = 0;
-    for (int x = 0; x < 5; ++x) W |= 1u << src.rows[x];
-    auto in_w = [&](int p) { return (W >> p & 1u) != 0; };
-    auto nxt = [&](int p) { return (next_lanes >> p & 1u) != 0; };
-    std::vector<int> Lw, Lo, Rw, Ro;
-    for (int p = 0; p < m; ++p) {
-        if (lanes >> p & 1u) (in_w(p) ? Lw : Lo).push_back(p);
-        else (in_w(p) ? Rw : Ro).push_back(p);
-    }
-    // Rows outside W: lanes outside the next block first (they keep the next
-    // block's choice free); W rows: lanes of the next block last.
-    std::stable_sort(Ro.begin(), Ro.end(), [&](int p, int q) { return !nxt(p) && nxt(q); });
-    TcLayout c;
-    for (int x = 0; x < 8; ++x) c.rows[x] = -1;
-    // amps: W lanes first (the first two are amps[0..1]).
-    std::vector<int> A(Lw);
-    A.insert(A.end(), Lo.begin(), Lo.end());
-    for (int k = 0; k < 5; ++k) c.amps[k] = A[k];
-    // rows[0..2]: a W row where amps[k + 2] is not a W lane, else a non-W row.
-    size_t iw = 0, io = 0;
-    std::vector<bool> used_o(Ro.size(), false);
-    for (int k = 0; k < 3; ++k) {
-        if (!in_w(c.amps[k + 2]) && iw < Rw.size()) {
-            c.rows[k] = Rw[iw++];
-        } else if (io < Ro.size()) {
-            used_o[io] = true;
-            c.rows[k] = Ro[io++];
-        } else {
-            c.rows[k] = Rw[iw++];
-        }
-    }
-    std::vector<int> rest;
-    for (; iw < Rw.size(); ++iw) rest.push_back(Rw[iw]);
-    for (size_t x = io; x < Ro.size(); ++x) rest.push_back(Ro[x]);
-    // rows[3..4]: top up to two lanes of the next block among rows[0..4].
-    int inext = 0;
-    for (int x = 0; x < 3; ++x) inext += nxt(c.rows[x]);
-    std::stable_sort(rest.begin(), rest.end(), [&](int p, int q) {
-        return inext < 2 ? (nxt(p) && !nxt(q)) : (!nxt(p) && nxt(q));
-    });
-    for (size_t x = 0; x < rest.size(); ++x) c.rows[3 + x] = rest[x];
-    return c;
-}
-
-// U (32x32, row-major) of a block's gates in the amplitude order of `lay`.
-static void tc_block_matrix(const std::vector<const PendingGate *> &gates, const TileLanes &tl,
-                            const TcLayout &lay, std::complex<double> *U) {
-    typedef std::complex<double> cd;
-    int bit_of[64];
-    for (int p = 0; p < 64; ++p) bit_of[p] = -1;
-    for (int k = 0; k < 5; ++k) bit_of[lay.amps[k]] = k;
-    for (int i = 0; i < 1024; ++i) U[i] = (i / 32 == i % 32) ? cd(1, 0) : cd(0, 0);
-    for (auto *g : gates) {
-        const int tb = 1 << bit_of[tl.local_of[g->target]];
-        int cm = 0;
-        for (int c : g->controls) cm |= 1 << bit_of[tl.local_of[c]];
-        const cd m00(g->m.v[0], g->m.v[1]), m01(g->m.v[2], g->m.v[3]), m10(g->m.v[4], g->m.v[5]),
-            m11(g->m.v[6], g->m.v[7]);
-        for (int r = 0; r < 32; ++r) {
-            if ((r & tb) || (r & cm) != cm) continue;
-            for (int c = 0; c < 32; ++c) {
-                cd a0 = U[r * 32 + c], a1 = U[(r | tb) * 32 + c];
-                U[r * 32 + c] = m00 * a0 + m01 * a1;
-                U[(r | tb) * 32 + c] = m10 * a0 + m11 * a1;
-            }
-        }
-    }
-}
-
-// Fills a block of fewer than 5 lanes: lanes of the source layout's warp
-// bits first (two of them keep its operand stores conflict-free), then the
-// lowest free positions.
-static unsigned tc_fill_lanes(unsigned lanes, const TcLayout &src, int m) {
-    for (int x = 0; x < 5 && __builtin_popcount(lanes) < 5; ++x) {
-        unsigned in_warp = 0;
-        for (int y = 0; y < 5; ++y) in_warp += lanes >> src.rows[y] & 1u;
-        if (in_warp >= 2) break;
-        lanes |= 1u << src.rows[x];
-    }
-    for (int p = 0; p < m && __builtin_popcount(lanes) < 5; ++p) lanes |= 1u << p;
-    return lanes;
-}
-
-// Shared-memory wavefronts of one warp-wide 4-byte store through slot
-// tables: the largest number of threads on one bank.
-static int tc_store_cost(const SetSlots &ss) {
-    int cnt[32] = {0};
-    int mx = 0;
-    for (int i = 0; i < 32; ++i) mx = std::max(mx, ++cnt[ss.lo[i] & 31]);
-    return mx;
-}
-
-// Wavefronts of one warp-wide 8-byte store through slot tables (two half
-// warps; per half, the largest number of threads on one 8-byte bank pair).
-static int tc_store_cost8(const SetSlots &ss) {
-    int cost = 0;
-    for (int h = 0; h < 2; ++h) {
-        int cnt[16] = {0}, mx = 0;
-        for (int i = 0; i < 16; ++i) mx = std::max(mx, ++cnt[ss.lo[16 * h + i] & 15]);
-        cost += mx;
-    }
-    return cost;
-}
-
-// Host plan of one tensor-stage launch: blocks [b0, b0 + nb) of a stage on
-// tile `tl` -> the descriptor (all but the operand pointer) and the split
-// block operands (nb x 2 x 4096 FP16 values) in `ops`.
-static void tc_plan_launch(const TileLanes &tl, int n,
-                           const std::vector<std::pair<unsigned, std::vector<const PendingGate *>>> &blocks,
-                           size_t b0, int nb, TcStageDesc &desc, unsigned short *ops) {
-    const int m = (int)tl.lanes.size();
-    const int t = m - 5;
-    const size_t kBlockHalves = 2 * 64 * 64;
-    memset(&desc, 0, sizeof(desc));
-    desc.n = n;
-    desc.m = m;
-    desc.nins = m < n ? m : 0;
-    for (int j = 0; j < desc.nins; ++j) desc.ins_pos[j] = tl.lanes[j];
-    desc.nblocks = nb;
-    // Load layout: tile positions 0..3 (the contiguous low lanes) plus one
-    // more position p on the warp's thread bits, chosen so that the first
-    // block's operand stores hit the fewest banks twice.
-    auto load_layout = [&](int p) {
-        TcLayout L;
-        for (int i = 0; i < 8; ++i) L.rows[i] = -1;
-        int r = 0, a = 0;
-        for (int q = 0; q < 4; ++q) L.rows[r++] = q;
-        L.rows[r++] = p;
-        for (int q = 4; q < m; ++q) {
-            if (q == p) continue;
-            if (a < 5) L.amps[a++] = q;
-            else L.rows[r++] = q;
-        }
-        return L;
-    };
-    TcLayout cur = load_layout(4);
-    {
-        unsigned lanes0 = tc_fill_lanes(blocks[b0].first, cur, m);
-        const unsigned next0 = nb > 1 ? blocks[b0 + 1].first : 0u;
-        int best = 1 << 30;
-        for (int p = 4; p < m; ++p) {
-            TcLayout L = load_layout(p);
-            unsigned l0 = tc_fill_lanes(blocks[b0].first, L, m);
-            TcLayout lay = tc_choose_layout(l0, next0, L, m);
-            int c = tc_store_cost(tc_slots(L, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); }));
-            if (c < best) {
-                best = c;
-                cur = L;
-                lanes0 = l0;
-            }
-        }
-        (void)lanes0;
-    }
-    for (int b = 0; b < t; ++b) desc.row_lane[b] = tl.lanes[cur.rows[b]];
-    for (int j = 0; j < 32; ++j) {
-        long long off = 0;
-        for (int k = 0; k < 5; ++k)
-            if (j >> k & 1) off |= 1LL << tl.lanes[cur.amps[k]];
-        desc.dep_hi[j] = off;
-    }
-    desc.sets[nb + 1] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
-    std::complex<double> U[1024];
-    for (int b = 0; b < nb; ++b) {
-        unsigned lanes = blocks[b0 + b].first;
-        lanes = tc_fill_lanes(lanes, cur, m);
-        const unsigned next = b + 1 < nb ? blocks[b0 + b + 1].first : 0u;
-        TcLayout lay = tc_choose_layout(lanes, next, cur, m);
-        if (b + 1 == nb) {
-            // Last block: rows[3..4] only feed the 8-byte stores into the
-            // natural tile; pick them for the fewest wavefronts there.
-            int best = 1 << 30;
-            TcLayout keep = lay;
-            for (int x = 3; x < t; ++x)
-                for (int y = 3; y < t; ++y) {
-                    if (x == y) continue;
-                    TcLayout c = keep;
-                    std::swap(c.rows[3], c.rows[x]);
-                    std::swap(c.rows[4], c.rows[y == 3 ? x : y]);
-                    const int cost = tc_store_cost8(
-                        tc_slots(c, t, [&](unsigned ti) { return host_swz(ti, kFP32); }));
-                    if (cost < best) {
-                        best = cost;
-                        lay = c;
-                    }
-                }
-        }
-        desc.sets[b] = tc_slots(cur, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); });
-        tc_block_matrix(blocks[b0 + b].second, tl, lay, U);
-        tc_compensate(U);
-        tc_operand(U, ops + b * kBlockHalves, ops + b * kBlockHalves + kBlockHalves / 2);
-        cur = lay;
-    }
-    desc.sets[nb] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
-}
-
 static void run_tstage(Device &d, States *s, const TileLanes &tl,
                        const std::vector<const PendingGate *> &gates) {
     const int n = s->n_lanes;
@@ -992,33 +603,6 @@ static int gate_cost(const PendingGate &g) {
     return 9;
 }
 
-// Gates of `gates` (in order) that a stage on lane set S takes: a gate is
-// taken when its lanes lie in S and no earlier gate that was left out shares
-// a lane with it (so it commutes with everything left out before it).  At
-// most `limit` gates are scanned and kMaxStageGates taken; returns the count.
-static int stage_take(const std::vector<const PendingGate *> &gates, unsigned long long S,
-                      size_t limit, std::vector<const PendingGate *> *take,
-                      std::vector<const PendingGate *> *keep) {
-    unsigned long long blocked = 0;
-    int count = 0;
-    for (size_t i = 0; i < gates.size(); ++i) {
-        const PendingGate *g = gates[i];
-        if (i >= limit) {
-            if (keep) keep->push_back(g);
-            continue;
-        }
-        const unsigned long long q = gate_qmask(*g);
-        if ((q & blocked) || (q & ~S) || count >= kMaxStageGates) {
-            blocked |= q;
-            if (keep) keep->push_back(g);
-            continue;
-        }
-        ++count;
-        if (take) take->push_back(g);
-    }
-    return count;
-}
-
 // Planner for tensor-core stages: instead of growing a stage's lane set in
 // gate order, it starts from the low lanes and the first pending gate's
 // lanes and adds, one at a time up to M lanes, the lane that lets the stage
@@ -1030,7 +614,6 @@ static int stage_take(const std::vector<const PendingGate *> &gates, unsigned lo
 static void flush_lookahead(Device &d, States *s, std::vector<const PendingGate *> &remaining,
                             unsigned long long base, int M, int max_stages = 1 << 30) {
     const int n = s->n_lanes;
-    const size_t kWindow = 512;
     for (int done = 0; !remaining.empty() && done < max_stages; ++done) {
         const unsigned long long q0 = gate_qmask(*remaining[0]);
         if (__builtin_popcountll(q0 | base) > M) {
@@ -1038,77 +621,7 @@ static void flush_lookahead(Device &d, States *s, std::vector<const PendingGate 
             remaining.erase(remaining.begin());
             continue;
         }
-        unsigned long long cand_all = 0;
-        for (size_t i = 0; i < remaining.size() && i < kWindow; ++i)
-            cand_all |= gate_qmask(*remaining[i]);
-        const unsigned long long fixed = base | q0;
-        // Greedy growth from `S0`: add the lane that lets the stage take the
-        // most gates until the stage has M lanes.
-        auto grow = [&](unsigned long long S0) {
-            unsigned long long S = S0;
-            while (__builtin_popcountll(S) < M) {
-                const unsigned long long cand = cand_all & ~S;
-                if (!cand) break;
-                int best = -1, best_lane = -1;
-                for (unsigned long long c = cand; c; c &= c - 1) {
-                    const int lane = __builtin_ctzll(c);
-                    const int got =
-                        stage_take(remaining, S | (1ULL << lane), kWindow, nullptr, nullptr);
-                    if (got > best) {
-                        best = got;
-                        best_lane = lane;
-                    }
-                }
-                S |= 1ULL << best_lane;
-            }
-            return S;
-        };
-        // Multi-start: the plain greedy growth, and growths seeded with each
-        // of the few lanes that take the most gates on their own; keep the
-        // best.
-        unsigned long long S = grow(fixed);
-        int cur = stage_take(remaining, S, kWindow, nullptr, nullptr);
-        {
-            std::vector<std::pair<int, int>> seeds;
-            for (unsigned long long c = cand_all & ~fixed; c; c &= c - 1) {
-                const int lane = __builtin_ctzll(c);
-                seeds.emplace_back(
-                    -stage_take(remaining, fixed | (1ULL << lane), kWindow, nullptr, nullptr), lane);
-            }
-            std::sort(seeds.begin(), seeds.end());
-            for (size_t k = 0; k < seeds.size() && k < 6 && __builtin_popcountll(fixed) < M; ++k) {
-                const unsigned long long T = grow(fixed | (1ULL << seeds[k].second));
-                const int got = stage_take(remaining, T, kWindow, nullptr, nullptr);
-                if (got > cur) {
-                    S = T;
-                    cur = got;
-                }
-            }
-        }
-        // Swap pass: replace a chosen lane (not a low lane or one of the
-        // first gate's) by an outside lane while that lets the stage take
-        // more gates.
-        {
-            const unsigned long long cand = cand_all;
-            for (int iter = 0; iter < 16; ++iter) {
-                bool improved = false;
-                for (unsigned long long o = S & ~fixed; o && !improved; o &= o - 1) {
-                    const unsigned long long out = o & (0ULL - o);
-                    for (unsigned long long c = cand & ~S; c; c &= c - 1) {
-                        const unsigned long long in = c & (0ULL - c);
-                        const unsigned long long T = (S & ~out) | in;
-                        const int got = stage_take(remaining, T, kWindow, nullptr, nullptr);
-                        if (got > cur) {
-                            S = T;
-                            cur = got;
-                            improved = true;
-                            break;
-                        }
-                    }
-                }
-                if (!improved) break;
-            }
-        }
+        unsigned long long S = plan_stage_lanes(remaining, base, M);
         std::vector<const PendingGate *> chosen, deferred;
         stage_take(remaining, S, remaining.size(), &chosen, &deferred);
         if (chosen.size() == 1) {

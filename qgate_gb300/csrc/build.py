@@ -21,7 +21,7 @@ LIB = os.path.join(PKG, 'libqgate_gb300.so')
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 CU_SOURCES = ['gates.cu', 'reduce.cu', 'fused.cu', 'adjoint.cu', 'batch.cu', 'noalloc.cu', 'tcstage.cu']
-CXX_SOURCES = ['api.cpp', 'adjoint_host.cpp']
+CXX_SOURCES = ['api.cpp', 'adjoint_host.cpp', 'tcplan.cpp']
 
 
 def _cuda_home():
