@@ -369,6 +369,10 @@ def run_gb300(args):
     if not args.no_e2e and rank == 0:
         e2e = run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2)
 
+    kernels = None
+    if rank == 0 and not args.no_e2e:
+        kernels = observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2)
+
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch(args, nat)
@@ -413,6 +417,7 @@ def run_gb300(args):
                 'circuit_ms': t_max / args.steps,
                 'gates_per_s': stats['gates'] / args.steps / (t_max / args.steps / 1e3)}),
             'roofline': roofline,
+            'observation_kernels': kernels,
             'accuracy': accuracy,
             'adjoint': adjoint,
             'batch': batch,
@@ -602,6 +607,69 @@ def run_batch(args, nat):
             'graph_ms': gms / max(1, launches), 'circuits_per_s_graph':
                 len(circuits) / (gms / max(1, launches) / 1e3),
             'amplitude_updates_per_s': amps / dt, 'checksum': float(np.sum(out))}
+
+
+def observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2):
+    """Per-kernel-class device time and HBM roofline of the observation path
+    on the final 2^n state: Pr(lane = 0) (prob), a Pauli expectation (pauli),
+    the full probability vector (gather), a sampling pool over all lanes (its
+    FP64 marginal and the two-pass FP64 prefix sum: marginal, scan), 1e7
+    samples (search) and the |0...0> reset (init).  CUDA events per launch on
+    the engine stream; algorithmic bytes = what each kernel must read and
+    write once."""
+    N = 1 << n
+    amp = cs
+    getter = rt.create_qubits_states_getter(dtype)
+    lanes = [(qs, [Lane(l, l) for l in range(n)])]
+    probs = np.empty(N, dtype)
+    u = np.random.default_rng(12).random(args.samples)
+    # warm the arena and the host buffers once, untimed
+    getter.get_states(probs, 0, abs2, lanes, [], N, 0, 1)
+    pool = getter.create_sampling_pool(list(range(n)), n, 0, lanes, [])
+    pool.sample(args.samples, u)
+    pool.delete()
+    nat.timing_all(reset=True)
+    nat.timing_enable(True)
+    proc.calc_probability(qs, 0)
+    proc.calc_probability(qs, n - 1)
+    proc.calc_pauli_expectation(qs, 1 << 3, (1 << 3) | (1 << 7))
+    getter.get_states(probs, 0, abs2, lanes, [], N, 0, 1)
+    pool = getter.create_sampling_pool(list(range(n)), n, 0, lanes, [])
+    pool.sample(args.samples, u)
+    pool.delete()
+    proc.reset_qubit_states(qs)
+    proc.synchronize()
+    nat.timing_enable(False)
+    tm = nat.timing_all(reset=True)
+    peak, kind = measured_peak_hbm()
+    # algorithmic bytes per launch (scan: per pool, both passes)
+    model = {
+        'prob': (N // 2 * amp, 'read the half of the state with the lane at 0'),
+        'pauli': (N * amp, 'read the state'),
+        'gather': (N * amp + N * (amp // 2), 'read the state, write 2^n probabilities'),
+        'marginal': (N * amp + N * 8, 'read the state, write 2^n FP64 probabilities'),
+        'scan': (3 * N * 8, 'two passes: read the FP64 array, then read and write it'),
+        'init': (N * amp, 'write the state'),
+    }
+    out = {}
+    for cls, (launches, ms) in tm.items():
+        if not launches:
+            continue
+        e = {'launches': launches, 'ms': ms}
+        per = ms / launches
+        if cls == 'scan':
+            per = ms  # one pool: its two launches
+        if cls in model:
+            b, what = model[cls]
+            gbs = b / (per / 1e3) / 1e9
+            e.update({'algorithmic_bytes': b, 'bytes_are': what, 'gbs': gbs,
+                      'frac_of_peak': gbs / peak})
+        if cls == 'search':
+            e['samples_per_s'] = args.samples / (ms / 1e3)
+        out[cls] = e
+    out['peak_gbs'] = peak
+    out['peak_source'] = kind
+    return out
 
 
 def run_e2e(args, rt, nat, qs, step, ops, n, cs, dtype, Lane, abs2):

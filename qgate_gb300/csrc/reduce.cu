@@ -203,6 +203,48 @@ k_gather(void *__restrict__ out, idx_t count, idx_t start, idx_t step,
     }
 }
 
+// Gather of one state in its own lane order over a contiguous range (the
+// common full probability vector / state dump): out[i] = op(psi[start + i]),
+// 4 items per thread with 16-byte loads where aligned.
+template <class R, int MATHOP>
+__global__ void __launch_bounds__(256)
+k_gather_contig(void *__restrict__ out, const typename CT<R>::type *__restrict__ psi,
+                idx_t count) {
+    typedef typename CT<R>::type C;
+    const idx_t stride = (idx_t)gridDim.x * blockDim.x;
+    const idx_t quads = count / 4;
+    for (idx_t q = (idx_t)blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += stride) {
+        const C a0 = psi[4 * q], a1 = psi[4 * q + 1], a2 = psi[4 * q + 2], a3 = psi[4 * q + 3];
+        if (MATHOP == 0) {
+            C *o = (C *)out + 4 * q;
+            o[0] = a0;
+            o[1] = a1;
+            o[2] = a2;
+            o[3] = a3;
+        } else if (sizeof(R) == 4) {
+            float4 p;
+            p.x = a0.x * a0.x + a0.y * a0.y;
+            p.y = a1.x * a1.x + a1.y * a1.y;
+            p.z = a2.x * a2.x + a2.y * a2.y;
+            p.w = a3.x * a3.x + a3.y * a3.y;
+            ((float4 *)out)[q] = p;
+        } else {
+            R *o = (R *)out + 4 * q;
+            o[0] = a0.x * a0.x + a0.y * a0.y;
+            o[1] = a1.x * a1.x + a1.y * a1.y;
+            o[2] = a2.x * a2.x + a2.y * a2.y;
+            o[3] = a3.x * a3.x + a3.y * a3.y;
+        }
+    }
+    for (idx_t i = 4 * quads + (idx_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        const C a = psi[i];
+        if (MATHOP == 0)
+            ((C *)out)[i] = a;
+        else
+            ((R *)out)[i] = a.x * a.x + a.y * a.y;
+    }
+}
+
 // Marginal probabilities: out[o] = sum_c prod_q |psi_q[local_q(o | c << n_lanes)]|^2,
 // FP64.  blockIdx.y splits the hidden range into groups written to scratch.
 template <class R>
@@ -408,6 +450,30 @@ void launch_pauli(int prec, const void *state, int n_lanes, unsigned long long x
 void launch_gather(int prec, int mathop, void *out, idx_t count, idx_t start, idx_t step,
                    unsigned long long empty_mask, const GatherDesc &g, cudaStream_t stream) {
     if (count <= 0) return;
+    bool contig = g.nqs == 1 && step == 1 && empty_mask == 0 && start >= 0 &&
+                  ((uintptr_t)out & 15u) == 0;
+    for (int l = g.lane_begin[0]; contig && l < g.lane_begin[1]; ++l)
+        contig = g.ext[l] == l - g.lane_begin[0];
+    // the range must stay inside the state: bits above its lanes are not read
+    contig = contig && start + count <= ((idx_t)1 << (g.lane_begin[1] - g.lane_begin[0]));
+    if (contig) {
+        const unsigned nq = sm_grid(count / 4 + 1, 256, 152 * 16);
+        if (prec == kFP32) {
+            const float2 *p = (const float2 *)g.ptr[0] + start;
+            if (mathop == 0)
+                k_gather_contig<float, 0><<<nq, 256, 0, stream>>>(out, p, count);
+            else
+                k_gather_contig<float, 1><<<nq, 256, 0, stream>>>(out, p, count);
+        } else {
+            const double2 *p = (const double2 *)g.ptr[0] + start;
+            if (mathop == 0)
+                k_gather_contig<double, 0><<<nq, 256, 0, stream>>>(out, p, count);
+            else
+                k_gather_contig<double, 1><<<nq, 256, 0, stream>>>(out, p, count);
+        }
+        QG_CUDA(cudaGetLastError());
+        return;
+    }
     unsigned nb = sm_grid(count, 256, 152 * 16);
     if (prec == kFP32) {
         if (mathop == 0)

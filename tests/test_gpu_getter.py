@@ -59,6 +59,26 @@ def test_get_states_permuted_empty_slices(rt, dtype):
 
 
 @pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_get_states_identity_ranges(rt, dtype):
+    """One state read in its own lane order (the streaming gather): whole
+    state, ranges with odd starts and lengths, single items, and outputs at
+    odd offsets of the caller's array."""
+    rng, states, psis = _build(rt, dtype, [9], 4)
+    qs, psi = states[0], psis[0]
+    N = 1 << 9
+    getter = rt.create_qubits_states_getter(dtype)
+    ident = [(qs, [Lane(l, l) for l in range(9)])]
+    for mathop, name in ((null, 'null'), (abs2, 'abs2')):
+        vd = (np.complex128 if dtype == np.float64 else np.complex64) if name == 'null' else dtype
+        for start, count in ((0, N), (1, N - 1), (3, 257), (N - 1, 1), (128, 7), (0, 5)):
+            for off in (0, 1, 3):
+                values = np.zeros(count + off, vd)
+                getter.get_states(values, off, mathop, ident, [], count, start, 1)
+                want = sv.get_states([(psi, list(range(9)))], name, count, start, 1, 0)
+                assert np.allclose(values[off:], want, atol=ATOL[dtype] * 2), (name, start, off)
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
 def test_get_states_range_errors(rt, dtype):
     _, states, _ = _build(rt, dtype, [3], 12)
     getter = rt.create_qubits_states_getter(dtype)
