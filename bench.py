@@ -612,8 +612,8 @@ def run_batch(args, nat):
 def observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2):
     """Per-kernel-class device time and HBM roofline of the observation path
     on the final 2^n state: Pr(lane = 0) (prob), a Pauli expectation (pauli),
-    the full probability vector (gather), a sampling pool over all lanes (its
-    FP64 marginal and the two-pass FP64 prefix sum: marginal, scan), 1e7
+    the full probability vector (gather), a sampling pool over all lanes (the
+    two-pass fixed-point prefix sum read straight from the state: scan), 1e7
     samples (search) and the |0...0> reset (init).  CUDA events per launch on
     the engine stream; algorithmic bytes = what each kernel must read and
     write once."""
@@ -648,7 +648,9 @@ def observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2):
         'pauli': (N * amp, 'read the state'),
         'gather': (N * amp + N * (amp // 2), 'read the state, write 2^n probabilities'),
         'marginal': (N * amp + N * 8, 'read the state, write 2^n FP64 probabilities'),
-        'scan': (3 * N * 8, 'two passes: read the FP64 array, then read and write it'),
+        'scan': (2 * N * amp + N * 8,
+                 'tile sums read the state; the scan reads it again and writes 2^n 64-bit '
+                 'prefix sums'),
         'init': (N * amp, 'write the state'),
     }
     out = {}

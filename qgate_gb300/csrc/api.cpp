@@ -126,7 +126,8 @@ struct Getter {
     int prec;
 };
 struct Pool {
-    double *cdf = nullptr;
+    unsigned long long *cdf = nullptr;  // fixed-point prefix sums, 2^-60 units
+    unsigned long long total = 0;       // cdf[n - 1]
     idx_t n = 0;
     std::vector<int> empty_pos;  // ascending
 };
@@ -1849,20 +1850,42 @@ int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_t
     Getter *g = lookup(g_dev.getters, hg, "getter");
     Device &d = dev();
     if (n_empty < 0 || n_lanes + n_empty > kMaxLanes) fail(QG_ERR_VALUE, "too many empty lanes.");
-    double *cdf = marginal_to_device(d, g, lane_tables, lane_counts, qstates_list, n_qstates,
-                                     n_lanes, n_hidden_lanes);
+    if (n_lanes < 0 || n_hidden_lanes < 0 || n_lanes + n_hidden_lanes > kMaxLanes)
+        fail(QG_ERR_VALUE, "lane counts out of range.");
     idx_t n = (idx_t)1 << n_lanes;
-    size_t sc = scan_scratch_doubles(n);
-    double *scratch = nullptr;
+    // One state in its own lane order with nothing summed out: the CDF is
+    // scanned straight from its amplitudes; otherwise from the FP64 marginal.
+    bool direct = n_qstates == 1 && n_hidden_lanes == 0 && lane_counts[0] == n_lanes;
+    for (int l = 0; direct && l < n_lanes; ++l) direct = lane_tables[l] == l;
+    unsigned long long *cdf = nullptr, *scratch = nullptr;
+    const void *src = nullptr;
+    if (direct) {
+        GatherDesc gd = make_gather(lane_tables, lane_counts, qstates_list, n_qstates, g->prec);
+        src = gd.ptr[0];
+        cdf = (unsigned long long *)d.arena.alloc(n * sizeof(unsigned long long));
+    } else {
+        cdf = (unsigned long long *)marginal_to_device(d, g, lane_tables, lane_counts,
+                                                       qstates_list, n_qstates, n_lanes,
+                                                       n_hidden_lanes);
+    }
+    unsigned long long total = 0;
     try {
-        scratch = (double *)d.arena.alloc(sc * sizeof(double));
-        double *d_total = d.d_partials + reduce_partials();
-        timed(d, "scan", [&] { launch_scan_sums(cdf, n, scratch, d_total, d.stream); });
-        double total = read_result(d, d_total);
+        scratch = (unsigned long long *)d.arena.alloc(pool_scratch_words(n) * 8);
+        const unsigned long long *d_total = nullptr;
+        timed(d, "scan", [&] {
+            d_total = direct ? launch_pool_cdf_state(g->prec, src, n, cdf, scratch, d.stream)
+                             : launch_pool_cdf_prob((const double *)cdf, n, cdf, scratch,
+                                                    d.stream);
+        });
+        QG_CUDA(cudaMemcpyAsync(d.h_result, d_total, 8, cudaMemcpyDeviceToHost, d.stream));
+        QG_CUDA(cudaStreamSynchronize(d.stream));
+        memcpy(&total, d.h_result, 8);
+        if (pool_status(true))
+            fail(QG_ERR_RUNTIME, "sampling-pool scan: a bounded wait for a bulk copy gave up.");
         // qgate/simulator/src/CPUSamplingPool.cpp:31-32
-        if (!(std::fabs(total - 1.) <= 0.05))
-            fail(QG_ERR_RUNTIME, "error in probability sum is beyond 0.05., %g.", total);
-        timed(d, "scan", [&] { launch_scan_apply(cdf, n, scratch, 1. / total, d.stream); });
+        double sum = std::ldexp((double)total, -60);
+        if (!(std::fabs(sum - 1.) <= 0.05))
+            fail(QG_ERR_RUNTIME, "error in probability sum is beyond 0.05., %g.", sum);
     } catch (...) {
         if (scratch) d.arena.release(scratch);
         d.arena.release(cdf);
@@ -1871,6 +1894,7 @@ int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_t
     d.arena.release(scratch);
     Pool *p = new Pool();
     p->cdf = cdf;
+    p->total = total;
     p->n = n;
     for (int i = 0; i < n_empty; ++i) p->empty_pos.push_back(empty_lanes[i]);
     std::sort(p->empty_pos.begin(), p->empty_pos.end());
@@ -1899,7 +1923,7 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
         try {
             QG_CUDA(cudaMemcpyAsync(du, randnum, bytes, cudaMemcpyHostToDevice, d.stream));
             timed(d, "search", [&] {
-                launch_search(p->cdf, p->n, du, dobs, n_samples, p->empty_pos.data(),
+                launch_search(p->cdf, p->n, p->total, du, dobs, n_samples, p->empty_pos.data(),
                               (int)p->empty_pos.size(), d.stream);
             });
             char *h = (char *)obs;
@@ -1930,7 +1954,7 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
             host_copy(d.h_stage[0], randnum + b, cnt * 8);
             QG_CUDA(cudaMemcpyAsync(du, d.h_stage[0], cnt * 8, cudaMemcpyHostToDevice, d.stream));
             timed(d, "search", [&] {
-                launch_search(p->cdf, p->n, du, dobs, cnt, p->empty_pos.data(),
+                launch_search(p->cdf, p->n, p->total, du, dobs, cnt, p->empty_pos.data(),
                               (int)p->empty_pos.size(), d.stream);
             });
             QG_CUDA(cudaMemcpyAsync(d.h_stage[1], dobs, cnt * 8, cudaMemcpyDeviceToHost, d.stream));

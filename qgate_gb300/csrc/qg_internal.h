@@ -343,14 +343,22 @@ void launch_marginal(int prec, double *out, int n_lanes, int n_hidden, const Gat
                      double *d_scratch, size_t scratch_doubles, cudaStream_t stream);
 size_t marginal_scratch_doubles(int n_lanes, int n_hidden);
 void launch_convert_f64(int prec, void *dst, const double *src, idx_t n, cudaStream_t stream);
-// In-place inclusive FP64 scan; returns the total through d_total.
-size_t scan_scratch_doubles(idx_t n);
-void launch_scan_sums(double *data, idx_t n, double *d_scratch, double *d_total,
-                      cudaStream_t stream);
-void launch_scan_apply(double *data, idx_t n, double *d_scratch, double norm,
-                       cudaStream_t stream);
-void launch_search(const double *cdf, idx_t n, const double *u, long long *obs, idx_t n_samples,
-                   const int *empty_pos, int n_empty, cudaStream_t stream);
+// Sampling-pool CDF: inclusive prefix sums of round(p * 2^60) as 64-bit
+// integers, from a state's |a|^2 in its own lane order or from an FP64
+// probability array (cdf may alias prob).  Both return the device address
+// of the total, which saturates at 2^64 - 1; pool_status reports a bounded
+// wait of the bulk-copy kernels that gave up.
+size_t pool_scratch_words(idx_t n);
+const unsigned long long *launch_pool_cdf_state(int prec, const void *state, idx_t n,
+                                                unsigned long long *cdf,
+                                                unsigned long long *scratch, cudaStream_t stream);
+const unsigned long long *launch_pool_cdf_prob(const double *prob, idx_t n,
+                                               unsigned long long *cdf,
+                                               unsigned long long *scratch, cudaStream_t stream);
+int pool_status(bool reset);
+void launch_search(const unsigned long long *cdf, idx_t n, unsigned long long total,
+                   const double *u, long long *obs, idx_t n_samples, const int *empty_pos,
+                   int n_empty, cudaStream_t stream);
 
 inline SetSlots make_set_slots(const int *rb, int rl, int m, int prec) {
     SetSlots ss;

@@ -6,6 +6,9 @@
 // qgate/simulator/src/CPUSamplingPool.cpp:16-49).  Reductions write one
 // partial per block and a single-block pass sums the partials in a fixed
 // order, so results are bit-reproducible run to run.
+#include <algorithm>
+
+#include "qg_bulk.cuh"
 #include "qg_device.cuh"
 
 namespace qg {
@@ -289,98 +292,391 @@ __global__ void k_convert(R *__restrict__ dst, const double *__restrict__ src, i
         dst[i] = (R)src[i];
 }
 
-// ------------------------------------------------------------ FP64 scan
+// ------------------------------------------------------------ pool CDF
+//
+// The sampling pool's cumulative distribution is held as 64-bit fixed-point
+// prefix sums.  Each probability p becomes q = round(p * 2^60) (exact for a
+// complex64 |a|^2 >= 2^-37 and a complex128 |a|^2 >= 2^-8, else within
+// 2^-61), and the prefix sums of q are integers: the scan rounds nowhere and
+// every summation order gives the same bits.  A uniform u then selects the
+// first i with P[i] > floor(u * T), T the total, which is the reference's
+// upper_bound over its normalised FP64 CDF (cumsum / sum,
+// qgate/simulator/src/CPUSamplingPool.cpp:16-49, 71-81) evaluated without
+// rounding.  Keeping the per-item work in integers keeps it off GB300's FP64
+// pipe (about 2 operations per clock per SM), which bounds an FP64 scan of
+// 2^30 items at several milliseconds.  Sums saturate at 2^64 - 1 instead of
+// wrapping, so a state far from unit norm still fails the norm check.
 
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr idx_t kScanTile = kScanThreads * kScanItems;
+constexpr int kFixBits = 60;                          // q = p * 2^60
+constexpr unsigned long long kFixCap = 1ull << 62;    // FP64 p >= 4 (and NaN) reads as this
 
-__global__ void __launch_bounds__(kScanThreads)
-k_tile_sums(const double *__restrict__ x, idx_t n, double *__restrict__ sums) {
-    const idx_t base = (idx_t)blockIdx.x * kScanTile;
-    double v = 0.;
-#pragma unroll
-    for (int j = 0; j < kScanItems; ++j) {
-        idx_t i = base + (idx_t)j * kScanThreads + threadIdx.x;
-        if (i < n) v += x[i];
-    }
-    v = block_sum(v);
-    if (threadIdx.x == 0) sums[blockIdx.x] = v;
+typedef unsigned long long u64;
+
+__device__ __forceinline__ u64 sat_add(u64 a, u64 b) {
+    const u64 s = a + b;
+    return s < a ? ~0ull : s;
 }
 
-// Inclusive scan of one tile in place, plus the inclusive prefix of the
-// preceding tiles (incl_sums[tile - 1]), times norm.  Shared memory is padded
-// by one double per 16 so that each thread's run of 16 consecutive items
-// falls in distinct banks.
+// round(p * 2^60) to nearest, ties to even, for 0 <= p < 4: with
+// x = p * 2^28 (exact), q = floor(x) * 2^32 + rint((x - floor(x)) * 2^32),
+// every step exact but the last rounding.  Both halves are single
+// conversions, so the per-item cost is a few FP32-pipe instructions.
+// p >= 16 saturates the high word; NaN reads as 0.
+__device__ __forceinline__ u64 fix_from_f32(float p) {
+    const float x = p * 268435456.f;  // 2^28
+    const float f = floorf(x);
+    const unsigned hi = __float2uint_rz(f);
+    const unsigned lo = __float2uint_rn((x - f) * 4294967296.f);  // < 2^32
+    return ((u64)hi << 32) | lo;
+}
+
+// round(p * 2^60) to nearest, ties to even; p = m * 2^(e - 1075).  Integer
+// work only: FP64 operations are scarce on GB300.  p >= 4 saturates at 2^62.
+__device__ __forceinline__ u64 fix_from_f64(double p) {
+    const u64 b = (u64)__double_as_longlong(p);
+    if ((b << 1) < (1ull << 53)) return 0;  // +-0 and subnormals
+    const int e = (int)(b >> 52);           // the sign bit lifts negative p into saturation
+    const u64 m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = e - (1075 - kFixBits);
+    if (sh >= 0) return sh <= 9 ? m << sh : kFixCap;  // m << 9 < 2^62: p < 4
+    const int r = -sh;
+    if (r > 53) return 0;  // p * 2^60 < 1/2
+    const u64 q = m >> r, rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+    return q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+}
+
+// floor(u * T) for 0 <= u (sign ignored: -0 reads as 0); u >= 1 gives 2^64 - 1.
+__device__ __forceinline__ u64 fix_target(double u, u64 total) {
+    const u64 b = (u64)__double_as_longlong(u) & ~(1ull << 63);
+    const int e = (int)(b >> 52);
+    if (e >= 1023) return ~0ull;
+    if (e == 0) return 0;  // u < 2^-1022: u * T < 1
+    const u64 m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const u64 lo = m * total, hi = __umul64hi(m, total);
+    const int sh = 1075 - e;  // u * T = (m * T) >> sh, sh >= 53
+    if (sh >= 128) return 0;
+    if (sh >= 64) return hi >> (sh - 64);
+    return (hi << (64 - sh)) | (lo >> sh);
+}
+
+// Item sources: the probability of item i as a fixed-point integer.
+struct SrcStateF32 {
+    const float2 *p;
+    __device__ __forceinline__ u64 operator()(idx_t i) const {
+        const float2 a = p[i];
+        return fix_from_f32(a.x * a.x + a.y * a.y);
+    }
+};
+struct SrcStateF64 {
+    const double2 *p;
+    __device__ __forceinline__ u64 operator()(idx_t i) const {
+        const double2 a = p[i];
+        return fix_from_f64(a.x * a.x + a.y * a.y);
+    }
+};
+struct SrcProbF64 {
+    const double *p;
+    __device__ __forceinline__ u64 operator()(idx_t i) const { return fix_from_f64(p[i]); }
+};
+struct SrcFix {
+    const u64 *p;
+    __device__ __forceinline__ u64 operator()(idx_t i) const { return p[i]; }
+};
+
+// Two 8-byte items from one 16-byte chunk of shared memory.
+struct PairStateF32 {  // two complex64 amplitudes
+    static __device__ __forceinline__ void get(uint4 c, u64 &q0, u64 &q1) {
+        const float x0 = __uint_as_float(c.x), y0 = __uint_as_float(c.y);
+        const float x1 = __uint_as_float(c.z), y1 = __uint_as_float(c.w);
+        q0 = fix_from_f32(x0 * x0 + y0 * y0);
+        q1 = fix_from_f32(x1 * x1 + y1 * y1);
+    }
+};
+struct PairProbF64 {  // two FP64 probabilities
+    static __device__ __forceinline__ void get(uint4 c, u64 &q0, u64 &q1) {
+        q0 = fix_from_f64(__hiloint2double((int)c.y, (int)c.x));
+        q1 = fix_from_f64(__hiloint2double((int)c.w, (int)c.z));
+    }
+};
+
+__device__ __forceinline__ u64 warp_incl_scan(u64 v, int lane) {
+    for (int o = 1; o < 32; o <<= 1) {
+        const u64 t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v = sat_add(v, t);
+    }
+    return v;
+}
+
+template <class Src>
+__global__ void __launch_bounds__(kScanThreads)
+k_fix_tile_sums(Src src, idx_t n, u64 *__restrict__ sums) {
+    __shared__ u64 warp_sums[kScanThreads / 32];
+    const idx_t base = (idx_t)blockIdx.x * kScanTile;
+    u64 q[kScanItems];
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        const idx_t i = base + (idx_t)j * kScanThreads + threadIdx.x;
+        q[j] = i < n ? src(i) : 0;
+    }
+    u64 v = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) v = sat_add(v, q[j]);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = sat_add(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) warp_sums[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u64 t = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) t = sat_add(t, warp_sums[w]);
+        sums[blockIdx.x] = t;
+    }
+}
+
+// Inclusive scan of one tile plus the inclusive prefix of the preceding
+// tiles (incl_sums[tile - 1]).  Items pass through shared memory so that each
+// thread scans a run of 16 consecutive ones; the padding of one word per 16
+// puts a half-warp's runs in distinct banks.  out may alias the source.
 __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 
+template <class Src>
 __global__ void __launch_bounds__(kScanThreads)
-k_tile_apply(double *__restrict__ x, idx_t n, const double *__restrict__ incl_sums, double norm) {
-    __shared__ double tile[kScanTile + kScanTile / 16];
-    __shared__ double warp_tot[kScanThreads / 32];
+k_fix_tile_apply(Src src, u64 *out, idx_t n, const u64 *__restrict__ incl_sums) {
+    __shared__ u64 tile[kScanTile + kScanTile / 16];
+    __shared__ u64 warp_tot[kScanThreads / 32];
     const idx_t base = (idx_t)blockIdx.x * kScanTile;
-    for (int j = 0; j < kScanItems; ++j) {
-        int li = j * kScanThreads + threadIdx.x;
-        idx_t i = base + li;
-        tile[pad16(li)] = i < n ? x[i] : 0.;
+    {
+        u64 q[kScanItems];
+#pragma unroll
+        for (int j = 0; j < kScanItems; ++j) {
+            const idx_t i = base + (idx_t)j * kScanThreads + threadIdx.x;
+            q[j] = i < n ? src(i) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < kScanItems; ++j) tile[pad16(j * kScanThreads + threadIdx.x)] = q[j];
     }
     __syncthreads();
-    double loc[kScanItems];
-    double run = 0.;
+    u64 loc[kScanItems];
+    u64 run = 0;
 #pragma unroll
     for (int j = 0; j < kScanItems; ++j) {
-        run += tile[pad16(threadIdx.x * kScanItems + j)];
+        run = sat_add(run, tile[pad16(threadIdx.x * kScanItems + j)]);
         loc[j] = run;
     }
-    // exclusive scan of thread totals
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double inc = run;
-    for (int o = 1; o < 32; o <<= 1) {
-        double t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u64 inc = warp_incl_scan(run, lane);
+    u64 excl = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) excl = 0;
     if (lane == 31) warp_tot[warp] = inc;
     __syncthreads();
-    double warp_off = 0.;
-    for (int w = 0; w < warp; ++w) warp_off += warp_tot[w];
-    double off = warp_off + inc - run;
-    if (blockIdx.x > 0) off += incl_sums[blockIdx.x - 1];
+    u64 off = blockIdx.x > 0 ? incl_sums[blockIdx.x - 1] : 0;
+    for (int w = 0; w < warp; ++w) off = sat_add(off, warp_tot[w]);
+    off = sat_add(off, excl);
 #pragma unroll
     for (int j = 0; j < kScanItems; ++j)
-        tile[pad16(threadIdx.x * kScanItems + j)] = (loc[j] + off) * norm;
+        tile[pad16(threadIdx.x * kScanItems + j)] = sat_add(loc[j], off);
     __syncthreads();
+#pragma unroll
     for (int j = 0; j < kScanItems; ++j) {
-        int li = j * kScanThreads + threadIdx.x;
-        idx_t i = base + li;
-        if (i < n) x[i] = tile[pad16(li)];
+        const idx_t i = base + (idx_t)j * kScanThreads + threadIdx.x;
+        if (i < n) out[i] = tile[pad16(j * kScanThreads + threadIdx.x)];
     }
 }
 
-__global__ void k_copy_last(const double *x, idx_t n, double *out) { *out = x[n - 1]; }
+// Level 0 of the scan for 8-byte items, as persistent CTAs (two per SM)
+// that stream 32 KB tiles (4096 items) through a 3-stage ring of shared
+// memory with bulk async copies.  Thread t owns the run of items
+// [16t, 16t + 16) of a tile: 8 chunks of 16 bytes, read in the rotated
+// order c = (k + t) mod 8 so that the 8 lanes of each shared-memory phase
+// hit distinct banks.  Waits are bounded; on a timeout the CTA records
+// g_pool_status, drains its outstanding copies and stops.
+constexpr int kBulkStages = 3;
+constexpr unsigned kTileBytes = (unsigned)kScanTile * 8u;
+constexpr size_t kBulkSmem = (size_t)kBulkStages * kTileBytes;
 
-// upper_bound(cdf, u) clamped to n-1, then zero bits inserted at the empty
-// lanes (qgate/simulator/src/CPUSamplingPool.cpp:71-81; spec:
-// qgate/simulator/pyruntime.py:303-321).
+__device__ unsigned g_pool_status;
+
+// Pass 1: tile sums (saturating).
+template <class Pair>
+__global__ void __launch_bounds__(kScanThreads, 2)
+k_pool_sums_bulk(const unsigned char *__restrict__ src, idx_t tiles, u64 *__restrict__ sums) {
+    extern __shared__ __align__(128) unsigned char ring[];
+    __shared__ __align__(8) u64 bar[kBulkStages];
+    __shared__ u64 red[2][kScanThreads / 32];
+    __shared__ int abort_sh;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const idx_t my = tiles > (idx_t)blockIdx.x ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int st = 0; st < kBulkStages; ++st) mbar_init(smem_u32(&bar[st]), 1);
+        mbar_fence_init();
+        abort_sh = 0;
+    }
+    __syncthreads();
+    idx_t issued = 0;
+    if (tid == 0)
+        for (; issued < my && issued < kBulkStages; ++issued)
+            bulk_load(smem_u32(ring + issued * kTileBytes),
+                      src + (size_t)(blockIdx.x + issued * gridDim.x) * kTileBytes, kTileBytes,
+                      smem_u32(&bar[issued]));
+    idx_t i = 0;
+    for (; i < my; ++i) {
+        const int st = (int)(i % kBulkStages);
+        if (!mbar_wait(smem_u32(&bar[st]), (unsigned)(i / kBulkStages) & 1u)) {
+            atomicOr(&g_pool_status, 1u);
+            abort_sh = 1;
+        }
+        const uint4 *row = (const uint4 *)(ring + st * kTileBytes) + 8 * tid;
+        u64 v = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            u64 q0, q1;
+            Pair::get(row[(k + tid) & 7], q0, q1);
+            v = sat_add(v, sat_add(q0, q1));
+        }
+        for (int o = 16; o > 0; o >>= 1) v = sat_add(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) red[i & 1][warp] = v;
+        __syncthreads();
+        if (abort_sh) break;
+        if (tid == 0) {
+            u64 t = 0;
+            for (int w = 0; w < kScanThreads / 32; ++w) t = sat_add(t, red[i & 1][w]);
+            sums[blockIdx.x + i * gridDim.x] = t;
+            if (issued < my) {  // the stage just read is free again
+                bulk_load(smem_u32(ring + st * kTileBytes),
+                          src + (size_t)(blockIdx.x + issued * gridDim.x) * kTileBytes,
+                          kTileBytes, smem_u32(&bar[st]));
+                ++issued;
+            }
+        }
+    }
+    if (tid == 0)
+        for (idx_t j = i; j < issued; ++j)  // copies still in flight after an abort
+            mbar_wait(smem_u32(&bar[j % kBulkStages]), (unsigned)(j / kBulkStages) & 1u);
+}
+
+// Pass 2: the inclusive scan of each tile plus incl_sums[tile - 1], written
+// back through shared memory and out with bulk stores.  The arithmetic wraps
+// modulo 2^64, which is exact whenever the saturating total of pass 1 passes
+// the norm check (all partial sums are then below 2^61).  In rotated order,
+// with R_k the running sum of the chunks visited before k and W the sum of
+// the chunks c0..7 (c0 = t mod 8, visited first), the exclusive prefix of
+// chunk c_k within the run is R_k + (total - W) before the wrap to chunk 0
+// and R_k - W after it.
+template <class Pair>
+__global__ void __launch_bounds__(kScanThreads, 2)
+k_pool_scan_bulk(const unsigned char *src, idx_t tiles, u64 *cdf, const u64 *__restrict__ incl_sums) {
+    extern __shared__ __align__(128) unsigned char ring[];
+    __shared__ __align__(8) u64 bar[kBulkStages];
+    __shared__ u64 red[2][kScanThreads / 32];
+    __shared__ int abort_sh;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, c0 = tid & 7;
+    const idx_t my = tiles > (idx_t)blockIdx.x ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int st = 0; st < kBulkStages; ++st) mbar_init(smem_u32(&bar[st]), 1);
+        mbar_fence_init();
+        abort_sh = 0;
+    }
+    __syncthreads();
+    // Two tiles ahead; the third stage is refilled once its store has read it.
+    idx_t issued = 0;
+    if (tid == 0)
+        for (; issued < my && issued < kBulkStages - 1; ++issued)
+            bulk_load(smem_u32(ring + issued * kTileBytes),
+                      src + (size_t)(blockIdx.x + issued * gridDim.x) * kTileBytes, kTileBytes,
+                      smem_u32(&bar[issued]));
+    idx_t i = 0;
+    for (; i < my; ++i) {
+        const idx_t tile = blockIdx.x + i * gridDim.x;
+        const u64 base = tile > 0 ? incl_sums[tile - 1] : 0;
+        const int st = (int)(i % kBulkStages);
+        if (!mbar_wait(smem_u32(&bar[st]), (unsigned)(i / kBulkStages) & 1u)) {
+            atomicOr(&g_pool_status, 1u);
+            abort_sh = 1;
+        }
+        uint4 *row = (uint4 *)(ring + st * kTileBytes) + 8 * tid;
+        u64 q[16], R[8];
+        u64 tot = 0, W = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            Pair::get(row[(k + tid) & 7], q[2 * k], q[2 * k + 1]);
+            R[k] = tot;
+            const u64 sk = q[2 * k] + q[2 * k + 1];
+            tot += sk;
+            if (k < 8 - c0) W += sk;
+        }
+        u64 inc = tot;
+        for (int o = 1; o < 32; o <<= 1) {
+            const u64 t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) red[i & 1][warp] = inc;
+        __syncthreads();
+        if (abort_sh) break;
+        u64 off = base + inc - tot;
+        for (int w = 0; w < warp; ++w) off += red[i & 1][w];
+        const u64 before = off + tot - W, after = off - W;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const u64 o0 = R[k] + (k < 8 - c0 ? before : after) + q[2 * k];
+            const u64 o1 = o0 + q[2 * k + 1];
+            row[(k + tid) & 7] = make_uint4((unsigned)o0, (unsigned)(o0 >> 32), (unsigned)o1,
+                                            (unsigned)(o1 >> 32));
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            bulk_store(cdf + (size_t)tile * kScanTile, smem_u32(ring + st * kTileBytes),
+                       kTileBytes);
+            bulk_commit();
+            if (issued < my) {
+                // stage issued % 3 last held tile i - 1: its store must have read it
+                if (issued >= kBulkStages) bulk_wait_read<1>();
+                const int sn = (int)(issued % kBulkStages);
+                bulk_load(smem_u32(ring + sn * kTileBytes),
+                          src + (size_t)(blockIdx.x + issued * gridDim.x) * kTileBytes,
+                          kTileBytes, smem_u32(&bar[sn]));
+                ++issued;
+            }
+        }
+    }
+    if (tid == 0) {
+        for (idx_t j = i; j < issued; ++j)  // copies still in flight after an abort
+            mbar_wait(smem_u32(&bar[j % kBulkStages]), (unsigned)(j / kBulkStages) & 1u);
+        bulk_wait<0>();
+    }
+}
+
+// upper_bound over the fixed-point CDF (first i with cdf[i] > floor(u * T)),
+// clamped to n-1, then zero bits inserted at the empty lanes
+// (qgate/simulator/src/CPUSamplingPool.cpp:71-81; spec:
+// qgate/simulator/pyruntime.py:303-321).  A negative or NaN u selects 0, as
+// the FP64 upper_bound does.
 struct EmptyPos {
     int n;
     int pos[kMaxLanes];
 };
 
 __global__ void __launch_bounds__(256)
-k_search(const double *__restrict__ cdf, idx_t n, const double *__restrict__ u,
+k_search(const u64 *__restrict__ cdf, idx_t n, u64 total, const double *__restrict__ u,
          long long *__restrict__ obs, idx_t m, EmptyPos ep) {
     const idx_t stride = (idx_t)gridDim.x * blockDim.x;
     for (idx_t i = (idx_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
-        double x = u[i];
-        idx_t lo = 0, hi = n;
-        while (lo < hi) {
-            idx_t mid = (lo + hi) >> 1;
-            if (cdf[mid] <= x)
-                lo = mid + 1;
-            else
-                hi = mid;
+        const double x = u[i];
+        idx_t lo = 0;
+        if (x >= 0.) {
+            const u64 t = fix_target(x, total);
+            idx_t hi = n;
+            while (lo < hi) {
+                const idx_t mid = (lo + hi) >> 1;
+                if (cdf[mid] <= t)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            if (lo > n - 1) lo = n - 1;
         }
-        if (lo > n - 1) lo = n - 1;
         obs[i] = insert_zeros(lo, ep.pos, ep.n);
     }
 }
@@ -538,7 +834,7 @@ void launch_convert_f64(int prec, void *dst, const double *src, idx_t n, cudaStr
     QG_CUDA(cudaGetLastError());
 }
 
-size_t scan_scratch_doubles(idx_t n) {
+size_t pool_scratch_words(idx_t n) {
     size_t total = 0;
     idx_t len = n;
     while (len > 1) {
@@ -549,36 +845,102 @@ size_t scan_scratch_doubles(idx_t n) {
     return total + 2;
 }
 
-// Inclusive scan of every level above `data`; level-0 tiles are applied
-// later by launch_scan_apply, once the caller knows the normalisation.
-void launch_scan_sums(double *data, idx_t n, double *d_scratch, double *d_total,
-                      cudaStream_t stream) {
-    idx_t tiles = (n + kScanTile - 1) / kScanTile;
-    double *sums = d_scratch;
-    k_tile_sums<<<(unsigned)tiles, kScanThreads, 0, stream>>>(data, n, sums);
+// Inclusive fixed-point scan of src into out (out may alias src's storage);
+// the tile sums of each level are scanned in place one level up.
+template <class Src>
+static void fix_scan(Src src, idx_t n, u64 *out, u64 *scratch, cudaStream_t stream) {
+    const idx_t tiles = (n + kScanTile - 1) / kScanTile;
+    u64 *sums = scratch;
     if (tiles > 1) {
-        double *next = d_scratch + tiles + 1;
-        launch_scan_sums(sums, tiles, next, nullptr, stream);
-        launch_scan_apply(sums, tiles, next, 1.0, stream);
+        k_fix_tile_sums<Src><<<(unsigned)tiles, kScanThreads, 0, stream>>>(src, n, sums);
+        fix_scan(SrcFix{sums}, tiles, sums, scratch + tiles + 1, stream);
     }
-    if (d_total) k_copy_last<<<1, 1, 0, stream>>>(sums, tiles, d_total);
+    k_fix_tile_apply<Src><<<(unsigned)tiles, kScanThreads, 0, stream>>>(src, out, n, sums);
     QG_CUDA(cudaGetLastError());
 }
 
-void launch_scan_apply(double *data, idx_t n, double *d_scratch, double norm,
-                       cudaStream_t stream) {
-    idx_t tiles = (n + kScanTile - 1) / kScanTile;
-    k_tile_apply<<<(unsigned)tiles, kScanThreads, 0, stream>>>(data, n, d_scratch, norm);
-    QG_CUDA(cudaGetLastError());
+static int sm_count() {
+    static int count = 0;
+    if (!count) {
+        int dev = 0;
+        QG_CUDA(cudaGetDevice(&dev));
+        QG_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
+    }
+    return count;
 }
 
-void launch_search(const double *cdf, idx_t n, const double *u, long long *obs, idx_t n_samples,
-                   const int *empty_pos, int n_empty, cudaStream_t stream) {
+// Level 0 by the bulk-copy kernels (8-byte items, whole tiles, 16-byte
+// aligned), upper levels by fix_scan.  Returns where the saturating total
+// ends up.
+template <class Pair>
+static const u64 *bulk_scan(const void *src, idx_t n, u64 *cdf, u64 *scratch,
+                            cudaStream_t stream) {
+    static bool configured = false;
+    if (!configured) {
+        QG_CUDA(cudaFuncSetAttribute(k_pool_sums_bulk<Pair>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBulkSmem));
+        QG_CUDA(cudaFuncSetAttribute(k_pool_scan_bulk<Pair>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBulkSmem));
+        configured = true;
+    }
+    const idx_t tiles = n / kScanTile;
+    const unsigned grid = (unsigned)std::min<idx_t>(tiles, 2 * (idx_t)sm_count());
+    u64 *sums = scratch;
+    k_pool_sums_bulk<Pair><<<grid, kScanThreads, kBulkSmem, stream>>>(
+        (const unsigned char *)src, tiles, sums);
+    if (tiles > 1) fix_scan(SrcFix{sums}, tiles, sums, scratch + tiles + 1, stream);
+    k_pool_scan_bulk<Pair><<<grid, kScanThreads, kBulkSmem, stream>>>(
+        (const unsigned char *)src, tiles, cdf, sums);
+    QG_CUDA(cudaGetLastError());
+    return sums + tiles - 1;
+}
+
+static bool bulk_ok(const void *p, idx_t n) {
+    return n >= kScanTile && n % kScanTile == 0 && ((uintptr_t)p & 15u) == 0;
+}
+
+const unsigned long long *launch_pool_cdf_state(int prec, const void *state, idx_t n,
+                                                unsigned long long *cdf,
+                                                unsigned long long *scratch,
+                                                cudaStream_t stream) {
+    if (prec == kFP32 && bulk_ok(state, n) && bulk_ok(cdf, n))
+        return bulk_scan<PairStateF32>(state, n, cdf, scratch, stream);
+    if (prec == kFP32)
+        fix_scan(SrcStateF32{(const float2 *)state}, n, cdf, scratch, stream);
+    else
+        fix_scan(SrcStateF64{(const double2 *)state}, n, cdf, scratch, stream);
+    return cdf + n - 1;
+}
+
+const unsigned long long *launch_pool_cdf_prob(const double *prob, idx_t n,
+                                               unsigned long long *cdf,
+                                               unsigned long long *scratch,
+                                               cudaStream_t stream) {
+    if (bulk_ok(prob, n) && bulk_ok(cdf, n))
+        return bulk_scan<PairProbF64>(prob, n, cdf, scratch, stream);
+    fix_scan(SrcProbF64{prob}, n, cdf, scratch, stream);
+    return cdf + n - 1;
+}
+
+int pool_status(bool reset) {
+    unsigned v = 0;
+    QG_CUDA(cudaMemcpyFromSymbol(&v, g_pool_status, sizeof(v)));
+    if (reset && v) {
+        unsigned z = 0;
+        QG_CUDA(cudaMemcpyToSymbol(g_pool_status, &z, sizeof(z)));
+    }
+    return (int)v;
+}
+
+void launch_search(const unsigned long long *cdf, idx_t n, unsigned long long total,
+                   const double *u, long long *obs, idx_t n_samples, const int *empty_pos,
+                   int n_empty, cudaStream_t stream) {
     if (n_samples <= 0) return;
     EmptyPos ep;
     ep.n = n_empty;
     for (int i = 0; i < n_empty; ++i) ep.pos[i] = empty_pos[i];
-    k_search<<<sm_grid(n_samples, 256, 152 * 16), 256, 0, stream>>>(cdf, n, u, obs, n_samples, ep);
+    k_search<<<sm_grid(n_samples, 256, 152 * 16), 256, 0, stream>>>(cdf, n, total, u, obs,
+                                                                   n_samples, ep);
     QG_CUDA(cudaGetLastError());
 }
 

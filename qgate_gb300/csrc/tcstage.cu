@@ -38,6 +38,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "qg_bulk.cuh"
 #include "qg_device.cuh"
 #include "qg_internal.h"
 #include "qg_regstage.cuh"
@@ -48,10 +49,6 @@ __device__ unsigned g_tc_status;
 
 namespace {
 
-
-__device__ __forceinline__ unsigned smem_u32(const void *p) {
-    return (unsigned)__cvta_generic_to_shared(p);
-}
 
 // Shared-memory matrix descriptor: start address, leading-dimension byte
 // offset (between core matrices along K; unused by swizzled K-major
@@ -80,33 +77,6 @@ __device__ __forceinline__ void mma_commit(unsigned bar) {
     asm volatile(
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
         : "memory");
-}
-
-__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(unsigned bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
-}
-
-// Bounded wait for the completion of the phase with the given parity.  Each
-// try suspends the thread until the phase completes or a 20 us hint runs
-// out, so waiting threads do not spin on the issue slots; at most 2^16
-// tries (about 1.3 s).
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-    for (int i = 0; i < (1 << 16); ++i) {
-        unsigned ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}\n"
-            : "=r"(ok)
-            : "r"(bar), "r"(parity), "r"(20000u)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
 }
 
 __device__ __forceinline__ void tc_fence_before() {

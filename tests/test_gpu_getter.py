@@ -165,6 +165,80 @@ def test_sampling_pool_empty_lanes_and_random(rt, dtype):
     assert np.all((got & ((1 << 0) | (1 << 4) | (1 << 8))) == 0)
 
 
+def _fixed_point_samples(probs, u):
+    """The pool's sampling rule on exact integers: q = round(p * 2^60) (to
+    nearest, ties to even; exact in float64 for float32 and float64 p), P =
+    prefix sums of q, index = first i with P[i] > floor(u * P[-1]), clamped
+    to n - 1; negative and NaN u give 0."""
+    q = np.rint(probs.astype(np.float64) * 2.0 ** 60).astype(np.uint64)
+    P = np.cumsum(q, dtype=np.uint64)
+    T = int(P[-1])
+    out = np.zeros(len(u), np.int64)
+    for k, v in enumerate(np.asarray(u, np.float64)):
+        if not v >= 0.:
+            continue
+        if v >= 1.:
+            out[k] = len(P) - 1
+            continue
+        num, den = abs(float(v)).as_integer_ratio()
+        t = (num * T) // den
+        out[k] = min(int(np.searchsorted(P, np.uint64(t), side='right')), len(P) - 1)
+    return out
+
+
+EDGE_U = [0.0, -0.0, 1.0, 1.5, -0.5, float('nan'), 5e-324, 1. - 2. ** -53, 0.5]
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_sampling_pool_fixed_point_exact(rt, dtype):
+    """Samples equal, bit for bit, the integer model of the pool's CDF built
+    from the engine's own probabilities, both for a pool read straight from
+    the state (lanes in order) and for one built from the marginal (lanes
+    reversed); and they agree with the oracle's FP64 pool except within
+    rounding of a CDF boundary."""
+    n = 14
+    rng, states, psis = _build(rt, dtype, [n], 21)
+    qs, psi = states[0], psis[0]
+    getter = rt.create_qubits_states_getter(dtype)
+    u = np.concatenate([rng.random(100000), EDGE_U])
+    for table in (list(range(n)), list(range(n))[::-1]):
+        lanes = [(qs, [Lane(l, e) for l, e in enumerate(table)])]
+        probs = np.empty(1 << n, dtype)
+        getter.get_states(probs, 0, abs2, lanes, [], 1 << n, 0, 1)
+        pool = getter.create_sampling_pool(list(range(n)), n, 0, lanes, [])
+        got = np.asarray(pool.sample(len(u), u).intarray)
+        pool.delete()
+        assert np.array_equal(got, _fixed_point_samples(probs, u)), table[:2]
+        prob_ref = sv.marginal_probabilities([(psi, table)], n, 0)
+        want = sv.SamplingPool(prob_ref).sample(u[:100000])
+        cdf_ref = np.cumsum(prob_ref) / prob_ref.sum()
+        cdf_eng = np.cumsum(probs.astype(np.float64))
+        near, tau = sv.boundary_tolerance_mask(cdf_ref, cdf_eng / cdf_eng[-1], u[:100000])
+        assert np.array_equal(got[:100000][~near], want[~near]), tau
+        assert np.mean(near) < 0.01, tau
+
+
+def test_sampling_pool_fixed_point_exact_25q(rt):
+    """A 25-qubit complex64 pool: 8192 tiles of 4096, so the prefix sums go
+    through three scan levels; samples equal the integer model exactly."""
+    n = 25
+    rng = np.random.default_rng(25)
+    qs = new_state(rt, n, np.float32)
+    ops = [('g', 'H', (), False, q, ()) for q in range(n)]
+    ops += random_ops(rng, n, 20, max_controls=1)
+    apply_ops(qs, ops)
+    getter = rt.create_qubits_states_getter(np.float32)
+    lanes = [(qs, [Lane(l, l) for l in range(n)])]
+    probs = np.empty(1 << n, np.float32)
+    getter.get_states(probs, 0, abs2, lanes, [], 1 << n, 0, 1)
+    u = np.concatenate([rng.random(20000), EDGE_U])
+    pool = getter.create_sampling_pool(list(range(n)), n, 0, lanes, [])
+    got = np.asarray(pool.sample(len(u), u).intarray)
+    pool.delete()
+    qs.delete()
+    assert np.array_equal(got, _fixed_point_samples(probs, u))
+
+
 def test_sampling_pool_rejects_unnormalised_state(rt):
     """|sum - 1| > 0.05 raises, as CPUSamplingPool does
     (qgate/simulator/src/CPUSamplingPool.cpp:31-32)."""
