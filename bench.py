@@ -631,6 +631,10 @@ def observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2):
     nat.timing_all(reset=True)
     nat.timing_enable(True)
     proc.calc_probability(qs, 0)
+    proc.synchronize()
+    nat.timing_enable(False)
+    lane0 = nat.timing_all(reset=True).get('prob', (0, 0.))
+    nat.timing_enable(True)
     proc.calc_probability(qs, n - 1)
     proc.calc_pauli_expectation(qs, 1 << 3, (1 << 3) | (1 << 7))
     getter.get_states(probs, 0, abs2, lanes, [], N, 0, 1)
@@ -644,7 +648,7 @@ def observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2):
     peak, kind = measured_peak_hbm()
     # algorithmic bytes per launch (scan: per pool, both passes)
     model = {
-        'prob': (N // 2 * amp, 'read the half of the state with the lane at 0'),
+        'prob': (N // 2 * amp, 'read the half of the state with the lane at 0 (lane n-1)'),
         'pauli': (N * amp, 'read the state'),
         'gather': (N * amp + N * (amp // 2), 'read the state, write 2^n probabilities'),
         'marginal': (N * amp + N * 8, 'read the state, write 2^n FP64 probabilities'),
@@ -669,6 +673,14 @@ def observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2):
         if cls == 'search':
             e['samples_per_s'] = args.samples / (ms / 1e3)
         out[cls] = e
+    if lane0[0]:
+        # lanes 0 and 1 split every 32-byte sector: the whole state crosses HBM
+        b = N * amp
+        gbs = b / (lane0[1] / 1e3) / 1e9
+        out['prob_lane0'] = {'launches': lane0[0], 'ms': lane0[1], 'bytes': b,
+                             'bytes_are': 'every 32-byte sector of the state (lane 0 splits '
+                                          'each sector)',
+                             'gbs': gbs, 'frac_of_peak': gbs / peak}
     out['peak_gbs'] = peak
     out['peak_source'] = kind
     return out

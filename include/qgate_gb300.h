@@ -259,9 +259,9 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
  * pre-sized pool, or loops that must not take the device-wide
  * synchronisation a cudaMalloc / cudaFree can imply.  It allocates nothing
  * and never touches the engine's own context: the reduction's per-block
- * partials go to a fixed 1024-double (8 KiB) device array that each GPU
+ * partials go to a fixed 2048-double (16 KiB) device array that each GPU
  * holds from library load until process exit.  The reduction uses at most
- * 608 of those partials for any state size; n_lanes must be in [1, 40] and
+ * 1216 of those partials for any state size; n_lanes must be in [1, 40] and
  * anything else is rejected with QG_ERR_VALUE.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that
  * device current, so make that first call before any stream capture.  All

@@ -128,6 +128,8 @@ struct Getter {
 struct Pool {
     unsigned long long *cdf = nullptr;  // fixed-point prefix sums, 2^-60 units
     unsigned long long total = 0;       // cdf[n - 1]
+    unsigned *guide = nullptr;          // guide table (nullptr: plain search)
+    int guide_shift = 0;
     idx_t n = 0;
     std::vector<int> empty_pos;  // ascending
 };
@@ -1869,17 +1871,47 @@ int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_t
                                                        n_hidden_lanes);
     }
     unsigned long long total = 0;
+    // Guide table: buckets of 2^(64 - n_lanes) CDF units, about 16 items each
+    // for a normalised state; entries cover totals up to (1 + 1/16) * 2^60,
+    // beyond the norm check's 1.05.
+    PoolGuide guide{};
+    void *guide_aux = nullptr;
+    const unsigned kLongCap = 1u << 16;
     try {
+        if (n_lanes >= 12 && n_lanes <= 32) {
+            guide.shift = 64 - n_lanes;
+            guide.nb = (((1ull << 60) + (1ull << 56)) >> guide.shift) + 2;
+            guide.g = (unsigned *)d.arena.alloc(guide.nb * sizeof(unsigned));
+            guide_aux = d.arena.alloc(16 + (size_t)kLongCap * sizeof(uint4));
+            guide.long_count = (unsigned *)guide_aux;
+            guide.long_list = (uint4 *)((char *)guide_aux + 16);
+            guide.long_cap = kLongCap;
+            QG_CUDA(cudaMemsetAsync(guide.long_count, 0, sizeof(unsigned), d.stream));
+        }
         scratch = (unsigned long long *)d.arena.alloc(pool_scratch_words(n) * 8);
         const unsigned long long *d_total = nullptr;
         timed(d, "scan", [&] {
-            d_total = direct ? launch_pool_cdf_state(g->prec, src, n, cdf, scratch, d.stream)
-                             : launch_pool_cdf_prob((const double *)cdf, n, cdf, scratch,
+            d_total = direct ? launch_pool_cdf_state(g->prec, src, n, cdf, scratch, guide,
+                                                     d.stream)
+                             : launch_pool_cdf_prob((const double *)cdf, n, cdf, scratch, guide,
                                                     d.stream);
         });
         QG_CUDA(cudaMemcpyAsync(d.h_result, d_total, 8, cudaMemcpyDeviceToHost, d.stream));
+        if (guide.g)
+            QG_CUDA(cudaMemcpyAsync(d.h_result + 1, guide.long_count, sizeof(unsigned),
+                                    cudaMemcpyDeviceToHost, d.stream));
         QG_CUDA(cudaStreamSynchronize(d.stream));
         memcpy(&total, d.h_result, 8);
+        if (guide.g) {
+            unsigned long_count = 0;
+            memcpy(&long_count, d.h_result + 1, sizeof(unsigned));
+            d.arena.release(guide_aux);
+            guide_aux = nullptr;
+            if (long_count > kLongCap) {  // too many long runs: search without the table
+                d.arena.release(guide.g);
+                guide.g = nullptr;
+            }
+        }
         if (pool_status(true))
             fail(QG_ERR_RUNTIME, "sampling-pool scan: a bounded wait for a bulk copy gave up.");
         // qgate/simulator/src/CPUSamplingPool.cpp:31-32
@@ -1888,6 +1920,8 @@ int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_t
             fail(QG_ERR_RUNTIME, "error in probability sum is beyond 0.05., %g.", sum);
     } catch (...) {
         if (scratch) d.arena.release(scratch);
+        if (guide_aux) d.arena.release(guide_aux);
+        if (guide.g) d.arena.release(guide.g);
         d.arena.release(cdf);
         throw;
     }
@@ -1895,6 +1929,8 @@ int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_t
     Pool *p = new Pool();
     p->cdf = cdf;
     p->total = total;
+    p->guide = guide.g;
+    p->guide_shift = guide.shift;
     p->n = n;
     for (int i = 0; i < n_empty; ++i) p->empty_pos.push_back(empty_lanes[i]);
     std::sort(p->empty_pos.begin(), p->empty_pos.end());
@@ -1923,7 +1959,8 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
         try {
             QG_CUDA(cudaMemcpyAsync(du, randnum, bytes, cudaMemcpyHostToDevice, d.stream));
             timed(d, "search", [&] {
-                launch_search(p->cdf, p->n, p->total, du, dobs, n_samples, p->empty_pos.data(),
+                launch_search(p->cdf, p->n, p->total, p->guide, p->guide_shift, du, dobs,
+                              n_samples, p->empty_pos.data(),
                               (int)p->empty_pos.size(), d.stream);
             });
             char *h = (char *)obs;
@@ -1954,7 +1991,8 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
             host_copy(d.h_stage[0], randnum + b, cnt * 8);
             QG_CUDA(cudaMemcpyAsync(du, d.h_stage[0], cnt * 8, cudaMemcpyHostToDevice, d.stream));
             timed(d, "search", [&] {
-                launch_search(p->cdf, p->n, p->total, du, dobs, cnt, p->empty_pos.data(),
+                launch_search(p->cdf, p->n, p->total, p->guide, p->guide_shift, du, dobs, cnt,
+                              p->empty_pos.data(),
                               (int)p->empty_pos.size(), d.stream);
             });
             QG_CUDA(cudaMemcpyAsync(d.h_stage[1], dobs, cnt * 8, cudaMemcpyDeviceToHost, d.stream));
@@ -1975,6 +2013,7 @@ int qg_sampling_pool_delete(qg_handle hp) {
     QG_BEGIN
     Pool *p = lookup(g_dev.pools, hp, "sampling pool");
     g_dev.arena.release(p->cdf);
+    if (p->guide) g_dev.arena.release(p->guide);
     g_dev.pools.erase(p);
     delete p;
     QG_END

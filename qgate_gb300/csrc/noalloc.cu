@@ -20,10 +20,10 @@ namespace qg {
 namespace {
 
 // Per-block FP64 partials of the probability reduction.  The reduction
-// launches at most reduce_partials() (608) blocks whatever the state size, so
-// 1024 doubles (8 KiB per GPU, held from module load until process exit)
+// launches at most reduce_partials() (1216) blocks whatever the state size, so
+// 2048 doubles (16 KiB per GPU, held from module load until process exit)
 // always suffice; the entry point still checks the bound.
-constexpr int kNoAllocPartials = 1024;
+constexpr int kNoAllocPartials = 2048;
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
 
 constexpr int kMaxDevices = 64;

@@ -16,8 +16,10 @@ namespace qg {
 namespace {
 
 constexpr int kRedThreads = 256;
-constexpr int kRedBlocks = 152 * 4;  // 4 resident CTAs on each of 152 SMs
-constexpr int kUnroll = 4;
+// 8 CTAs of 256 threads on each of 152 SMs and 8 loads in flight per thread
+// before any arithmetic: enough bytes in flight to cover HBM latency.
+constexpr int kRedBlocks = 152 * 8;
+constexpr int kUnroll = 8;
 
 __device__ __forceinline__ double block_sum(double v) {
     __shared__ double warp_sums[32];
@@ -386,6 +388,63 @@ struct SrcFix {
     __device__ __forceinline__ u64 operator()(idx_t i) const { return p[i]; }
 };
 
+// Guide table of a pool (Chen and Asau's guide-table method for inverse
+// transform sampling): g[b] = the first i with P[i] > b * 2^shift, for the
+// nb buckets with b * 2^shift below the total.  Buckets hold about 16 items
+// on average, so a sample reads g[b], g[b + 1] and searches the few items
+// between them instead of the whole CDF.  Item i with inclusive prefix P[i]
+// and probability q starts the buckets ceil((P[i] - q) / 2^shift) ..
+// (P[i] - 1) >> shift; the scan writes up to 8 of them inline and appends
+// longer runs to a bounded list that k_guide_long fills (count > cap: the
+// pool searches without the table).
+typedef PoolGuide Guide;
+
+// floor((incl - 1) / 2^shift) for shift >= 32, -1 for incl == 0: the bucket
+// of the last CDF unit an item with inclusive prefix incl reaches.  Item i
+// starts the buckets (bucket(P[i-1]), bucket(P[i])].
+__device__ __forceinline__ int guide_bucket(u64 incl, int shift) {
+    return (int)((incl - 1) >> 32) >> (shift - 32);
+}
+
+// Buckets b0..b1 of item i, when there is more than one (or bad bounds).
+__device__ __noinline__ void guide_mark_slow(const Guide gd, unsigned i, long long b0,
+                                             long long b1) {
+    if (b0 < 0) b0 = 0;
+    if (b1 >= (long long)gd.nb) b1 = (long long)gd.nb - 1;
+    if (b0 > b1) return;
+    const long long inl = b1 - b0 < 8 ? b1 : b0 + 7;
+    for (long long b = b0; b <= inl; ++b) gd.g[b] = i;
+    if (inl < b1) {
+        const unsigned slot = atomicAdd(gd.long_count, 1u);
+        if (slot < gd.long_cap)
+            gd.long_list[slot] = make_uint4((unsigned)(inl + 1), (unsigned)((inl + 1) >> 32),
+                                            (unsigned)b1, i);
+    }
+}
+
+// Item i's bucket b after the previous item's bucket bp: usually equal (no
+// bucket starts here) or one more (one store).
+__device__ __forceinline__ void guide_mark(const Guide &gd, idx_t i, int bp, int b) {
+    if (b == bp) return;
+    if (b == bp + 1 && (unsigned)b < gd.nb)
+        gd.g[b] = (unsigned)i;
+    else
+        guide_mark_slow(gd, (unsigned)i, (long long)bp + 1, b);
+}
+
+// Fills the long runs: every thread of the grid walks the list.
+__global__ void __launch_bounds__(256)
+k_guide_long(Guide gd) {
+    const unsigned count = min(*gd.long_count, gd.long_cap);
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (unsigned j = 0; j < count; ++j) {
+        const uint4 e = gd.long_list[j];
+        const u64 b0 = (u64)e.x | ((u64)e.y << 32), b1 = e.z;
+        for (u64 b = b0 + (u64)blockIdx.x * blockDim.x + threadIdx.x; b <= b1; b += stride)
+            gd.g[b] = e.w;
+    }
+}
+
 // Two 8-byte items from one 16-byte chunk of shared memory.
 struct PairStateF32 {  // two complex64 amplitudes
     static __device__ __forceinline__ void get(uint4 c, u64 &q0, u64 &q1) {
@@ -443,7 +502,7 @@ __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 
 template <class Src>
 __global__ void __launch_bounds__(kScanThreads)
-k_fix_tile_apply(Src src, u64 *out, idx_t n, const u64 *__restrict__ incl_sums) {
+k_fix_tile_apply(Src src, u64 *out, idx_t n, const u64 *__restrict__ incl_sums, Guide gd) {
     __shared__ u64 tile[kScanTile + kScanTile / 16];
     __shared__ u64 warp_tot[kScanThreads / 32];
     const idx_t base = (idx_t)blockIdx.x * kScanTile;
@@ -474,9 +533,18 @@ k_fix_tile_apply(Src src, u64 *out, idx_t n, const u64 *__restrict__ incl_sums) 
     u64 off = blockIdx.x > 0 ? incl_sums[blockIdx.x - 1] : 0;
     for (int w = 0; w < warp; ++w) off = sat_add(off, warp_tot[w]);
     off = sat_add(off, excl);
+    int bp = gd.g ? guide_bucket(off, gd.shift) : 0;
 #pragma unroll
-    for (int j = 0; j < kScanItems; ++j)
-        tile[pad16(threadIdx.x * kScanItems + j)] = sat_add(loc[j], off);
+    for (int j = 0; j < kScanItems; ++j) {
+        const int li = threadIdx.x * kScanItems + j;
+        const u64 incl = sat_add(loc[j], off);
+        if (gd.g && base + li < n) {
+            const int b = guide_bucket(incl, gd.shift);
+            guide_mark(gd, base + li, bp, b);
+            bp = b;
+        }
+        tile[pad16(li)] = incl;
+    }
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kScanItems; ++j) {
@@ -566,7 +634,8 @@ k_pool_sums_bulk(const unsigned char *__restrict__ src, idx_t tiles, u64 *__rest
 // and R_k - W after it.
 template <class Pair>
 __global__ void __launch_bounds__(kScanThreads, 2)
-k_pool_scan_bulk(const unsigned char *src, idx_t tiles, u64 *cdf, const u64 *__restrict__ incl_sums) {
+k_pool_scan_bulk(const unsigned char *src, idx_t tiles, u64 *cdf, const u64 *__restrict__ incl_sums,
+                 Guide gd) {
     extern __shared__ __align__(128) unsigned char ring[];
     __shared__ __align__(8) u64 bar[kBulkStages];
     __shared__ u64 red[2][kScanThreads / 32];
@@ -617,12 +686,28 @@ k_pool_scan_bulk(const unsigned char *src, idx_t tiles, u64 *cdf, const u64 *__r
         u64 off = base + inc - tot;
         for (int w = 0; w < warp; ++w) off += red[i & 1][w];
         const u64 before = off + tot - W, after = off - W;
+        int bq[16];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const u64 o0 = R[k] + (k < 8 - c0 ? before : after) + q[2 * k];
             const u64 o1 = o0 + q[2 * k + 1];
+            bq[2 * k] = guide_bucket(o0, gd.shift);
+            bq[2 * k + 1] = guide_bucket(o1, gd.shift);
             row[(k + tid) & 7] = make_uint4((unsigned)o0, (unsigned)(o0 >> 32), (unsigned)o1,
                                             (unsigned)(o1 >> 32));
+        }
+        if (gd.g) {
+            // the item before chunk c's first is chunk c - 1's second (rotated
+            // position k - 1), or the run's start for chunk 0
+            const int brun = guide_bucket(off, gd.shift);
+            const idx_t first = tile * kScanTile + 16 * tid;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int c = (k + tid) & 7;
+                const int bp = c == 0 ? brun : bq[2 * ((k + 7) & 7) + 1];
+                guide_mark(gd, first + 2 * c, bp, bq[2 * k]);
+                guide_mark(gd, first + 2 * c + 1, bq[2 * k], bq[2 * k + 1]);
+            }
         }
         fence_async_smem();
         __syncthreads();
@@ -658,14 +743,34 @@ struct EmptyPos {
     int pos[kMaxLanes];
 };
 
+// With a guide table, t = floor(u * T) < T lies in bucket b = t >> shift <=
+// bmax = (T - 1) >> shift; the answer is in [g[b], g[b + 1]] (g[b + 1] read
+// as n - 1 past bmax), where cdf[hi] > t holds, so a lower-bound search over
+// that range finds it.
 __global__ void __launch_bounds__(256)
-k_search(const u64 *__restrict__ cdf, idx_t n, u64 total, const double *__restrict__ u,
-         long long *__restrict__ obs, idx_t m, EmptyPos ep) {
+k_search(const u64 *__restrict__ cdf, idx_t n, u64 total, const unsigned *__restrict__ guide,
+         int shift, const double *__restrict__ u, long long *__restrict__ obs, idx_t m,
+         EmptyPos ep) {
     const idx_t stride = (idx_t)gridDim.x * blockDim.x;
+    const u64 bmax = (total - 1) >> shift;
     for (idx_t i = (idx_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
         const double x = u[i];
         idx_t lo = 0;
-        if (x >= 0.) {
+        if (x >= 1.) {
+            lo = n - 1;
+        } else if (guide && x >= 0.) {
+            const u64 t = fix_target(x, total);
+            const u64 b = t >> shift;
+            lo = guide[b];
+            idx_t hi = b + 1 <= bmax ? (idx_t)guide[b + 1] : n - 1;
+            while (lo < hi) {
+                const idx_t mid = (lo + hi) >> 1;
+                if (cdf[mid] <= t)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+        } else if (x >= 0.) {
             const u64 t = fix_target(x, total);
             idx_t hi = n;
             while (lo < hi) {
@@ -848,14 +953,20 @@ size_t pool_scratch_words(idx_t n) {
 // Inclusive fixed-point scan of src into out (out may alias src's storage);
 // the tile sums of each level are scanned in place one level up.
 template <class Src>
-static void fix_scan(Src src, idx_t n, u64 *out, u64 *scratch, cudaStream_t stream) {
+static void fix_scan(Src src, idx_t n, u64 *out, u64 *scratch, const Guide &gd,
+                     cudaStream_t stream) {
     const idx_t tiles = (n + kScanTile - 1) / kScanTile;
     u64 *sums = scratch;
     if (tiles > 1) {
         k_fix_tile_sums<Src><<<(unsigned)tiles, kScanThreads, 0, stream>>>(src, n, sums);
-        fix_scan(SrcFix{sums}, tiles, sums, scratch + tiles + 1, stream);
+        fix_scan(SrcFix{sums}, tiles, sums, scratch + tiles + 1, Guide{}, stream);
     }
-    k_fix_tile_apply<Src><<<(unsigned)tiles, kScanThreads, 0, stream>>>(src, out, n, sums);
+    k_fix_tile_apply<Src><<<(unsigned)tiles, kScanThreads, 0, stream>>>(src, out, n, sums, gd);
+    QG_CUDA(cudaGetLastError());
+}
+
+static void guide_long(const Guide &gd, cudaStream_t stream) {
+    if (gd.g) k_guide_long<<<152 * 4, 256, 0, stream>>>(gd);
     QG_CUDA(cudaGetLastError());
 }
 
@@ -873,7 +984,7 @@ static int sm_count() {
 // aligned), upper levels by fix_scan.  Returns where the saturating total
 // ends up.
 template <class Pair>
-static const u64 *bulk_scan(const void *src, idx_t n, u64 *cdf, u64 *scratch,
+static const u64 *bulk_scan(const void *src, idx_t n, u64 *cdf, u64 *scratch, const Guide &gd,
                             cudaStream_t stream) {
     static bool configured = false;
     if (!configured) {
@@ -888,10 +999,11 @@ static const u64 *bulk_scan(const void *src, idx_t n, u64 *cdf, u64 *scratch,
     u64 *sums = scratch;
     k_pool_sums_bulk<Pair><<<grid, kScanThreads, kBulkSmem, stream>>>(
         (const unsigned char *)src, tiles, sums);
-    if (tiles > 1) fix_scan(SrcFix{sums}, tiles, sums, scratch + tiles + 1, stream);
+    if (tiles > 1) fix_scan(SrcFix{sums}, tiles, sums, scratch + tiles + 1, Guide{}, stream);
     k_pool_scan_bulk<Pair><<<grid, kScanThreads, kBulkSmem, stream>>>(
-        (const unsigned char *)src, tiles, cdf, sums);
+        (const unsigned char *)src, tiles, cdf, sums, gd);
     QG_CUDA(cudaGetLastError());
+    guide_long(gd, stream);
     return sums + tiles - 1;
 }
 
@@ -902,23 +1014,25 @@ static bool bulk_ok(const void *p, idx_t n) {
 const unsigned long long *launch_pool_cdf_state(int prec, const void *state, idx_t n,
                                                 unsigned long long *cdf,
                                                 unsigned long long *scratch,
-                                                cudaStream_t stream) {
+                                                const PoolGuide &gd, cudaStream_t stream) {
     if (prec == kFP32 && bulk_ok(state, n) && bulk_ok(cdf, n))
-        return bulk_scan<PairStateF32>(state, n, cdf, scratch, stream);
+        return bulk_scan<PairStateF32>(state, n, cdf, scratch, gd, stream);
     if (prec == kFP32)
-        fix_scan(SrcStateF32{(const float2 *)state}, n, cdf, scratch, stream);
+        fix_scan(SrcStateF32{(const float2 *)state}, n, cdf, scratch, gd, stream);
     else
-        fix_scan(SrcStateF64{(const double2 *)state}, n, cdf, scratch, stream);
+        fix_scan(SrcStateF64{(const double2 *)state}, n, cdf, scratch, gd, stream);
+    guide_long(gd, stream);
     return cdf + n - 1;
 }
 
 const unsigned long long *launch_pool_cdf_prob(const double *prob, idx_t n,
                                                unsigned long long *cdf,
                                                unsigned long long *scratch,
-                                               cudaStream_t stream) {
+                                               const PoolGuide &gd, cudaStream_t stream) {
     if (bulk_ok(prob, n) && bulk_ok(cdf, n))
-        return bulk_scan<PairProbF64>(prob, n, cdf, scratch, stream);
-    fix_scan(SrcProbF64{prob}, n, cdf, scratch, stream);
+        return bulk_scan<PairProbF64>(prob, n, cdf, scratch, gd, stream);
+    fix_scan(SrcProbF64{prob}, n, cdf, scratch, gd, stream);
+    guide_long(gd, stream);
     return cdf + n - 1;
 }
 
@@ -933,13 +1047,13 @@ int pool_status(bool reset) {
 }
 
 void launch_search(const unsigned long long *cdf, idx_t n, unsigned long long total,
-                   const double *u, long long *obs, idx_t n_samples, const int *empty_pos,
-                   int n_empty, cudaStream_t stream) {
+                   const unsigned *guide, int shift, const double *u, long long *obs,
+                   idx_t n_samples, const int *empty_pos, int n_empty, cudaStream_t stream) {
     if (n_samples <= 0) return;
     EmptyPos ep;
     ep.n = n_empty;
     for (int i = 0; i < n_empty; ++i) ep.pos[i] = empty_pos[i];
-    k_search<<<sm_grid(n_samples, 256, 152 * 16), 256, 0, stream>>>(cdf, n, total, u, obs,
+    k_search<<<sm_grid(n_samples, 256, 152 * 16), 256, 0, stream>>>(cdf, n, total, guide, shift, u, obs,
                                                                    n_samples, ep);
     QG_CUDA(cudaGetLastError());
 }

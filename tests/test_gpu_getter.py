@@ -239,6 +239,35 @@ def test_sampling_pool_fixed_point_exact_25q(rt):
     assert np.array_equal(got, _fixed_point_samples(probs, u))
 
 
+@pytest.mark.parametrize('n, n_h, flips', [(14, 0, [3]), (20, 12, [15]), (25, 17, [20])],
+                         ids=['basis14', 'h12of20', 'h17of25'])
+def test_sampling_pool_guide_long_runs(rt, n, n_h, flips):
+    """States whose items each span many guide buckets: a basis state (one
+    item covers every bucket), H on 12 of 20 lanes (4096 items of 16
+    buckets: the bounded list of long runs) and H on 17 of 25 lanes (2^17
+    long runs: more than the list holds, so the pool searches without the
+    table).  Samples equal the integer model exactly."""
+    qs = new_state(rt, n, np.float32)
+    ops = [('g', 'H', (), False, q, ()) for q in range(n_h)]
+    ops += [('g', 'X', (), False, q, ()) for q in flips]
+    apply_ops(qs, ops)
+    getter = rt.create_qubits_states_getter(np.float32)
+    lanes = [(qs, [Lane(l, l) for l in range(n)])]
+    probs = np.empty(1 << n, np.float32)
+    getter.get_states(probs, 0, abs2, lanes, [], 1 << n, 0, 1)
+    rng = np.random.default_rng(n)
+    u = np.concatenate([rng.random(20000), EDGE_U, (np.arange(64) + 0.5) / 64])
+    pool = getter.create_sampling_pool(list(range(n)), n, 0, lanes, [])
+    got = np.asarray(pool.sample(len(u), u).intarray)
+    pool.delete()
+    qs.delete()
+    assert np.array_equal(got, _fixed_point_samples(probs, u))
+    if n_h == 0:  # uniforms in [0, 1) select the basis state; >= 1: n - 1; < 0, NaN: 0
+        ok = (u >= 0.) & (u < 1.)
+        assert np.all(got[ok] == sum(1 << q for q in flips))
+        assert np.all(got[u >= 1.] == (1 << n) - 1) and np.all(got[~(u >= 0.)] == 0)
+
+
 def test_sampling_pool_rejects_unnormalised_state(rt):
     """|sum - 1| > 0.05 raises, as CPUSamplingPool does
     (qgate/simulator/src/CPUSamplingPool.cpp:31-32)."""
