@@ -139,13 +139,12 @@ template <class R>
 __global__ void __launch_bounds__(kRedThreads)
 k_pauli_pair(const typename CT<R>::type *__restrict__ s, idx_t n_items, int hbit,
              unsigned long long x_mask, unsigned long long z_mask, int ny, double *partials) {
+    typedef typename CT<R>::type C;
     double acc = 0.;
     const idx_t stride = (idx_t)gridDim.x * blockDim.x;
     idx_t k = (idx_t)blockIdx.x * blockDim.x + threadIdx.x;
-    auto term = [&](idx_t kk) -> R {
-        idx_t b = insert_zero(kk, hbit);
-        idx_t b2 = b ^ (idx_t)x_mask;
-        typename CT<R>::type p = s[b], q = s[b2];
+    auto term = [&](idx_t b, C p, C q) -> R {
+        const idx_t b2 = b ^ (idx_t)x_mask;
         R wr = q.x * p.x + q.y * p.y;
         R wi = q.x * p.y - q.y * p.x;
         R s1 = parity_sign_r<R>(b & (idx_t)z_mask), s2 = parity_sign_r<R>(b2 & (idx_t)z_mask);
@@ -157,12 +156,24 @@ k_pauli_pair(const typename CT<R>::type *__restrict__ s, idx_t n_items, int hbit
         }
     };
     for (; k + (kUnroll - 1) * stride < n_items; k += kUnroll * stride) {
+        // all loads first: 2 x kUnroll amplitudes in flight per thread
+        idx_t b[kUnroll];
+        C p[kUnroll], q[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            b[u] = insert_zero(k + u * stride, hbit);
+            p[u] = s[b[u]];
+            q[u] = s[b[u] ^ (idx_t)x_mask];
+        }
         R part = 0;
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) part += term(k + u * stride);
+        for (int u = 0; u < kUnroll; ++u) part += term(b[u], p[u], q[u]);
         acc += (double)part;
     }
-    for (; k < n_items; k += stride) acc += (double)term(k);
+    for (; k < n_items; k += stride) {
+        const idx_t b = insert_zero(k, hbit);
+        acc += (double)term(b, s[b], s[b ^ (idx_t)x_mask]);
+    }
     acc = block_sum(acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
