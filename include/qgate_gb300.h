@@ -172,6 +172,13 @@ int qg_set_host_direct(int on);
  * copy into the caller's buffer, after touching its pages with all host
  * threads; 0 stages them through pinned buffers in 64 MiB pieces. */
 int qg_set_pageable_copy(int on);
+/* Extension: layout of the sampling pools' guide tables created from now on.
+ * -1 (default): entries hold the exact item index and buckets span ~16 items
+ * up to 2^32 items; above that (33-34 lanes) entries hold index >> (lanes -
+ * 32) and buckets span ~64 items.  k in [0, 8] forces entries of index >> k
+ * (buckets of ~64 items when k > 0) at any size, which exercises the large-
+ * pool layout on small states.  Samples are identical either way. */
+int qg_set_pool_guide_index_shift(int k);
 /* Extension: status word of the tensor-core stage kernels after a
  * synchronize: 0 = every bounded wait completed; nonzero = a wait gave up
  * (that stage's tiles were left unchanged).  reset != 0 clears it. */

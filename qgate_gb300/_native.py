@@ -60,6 +60,7 @@ SIGNATURES = {
     'qg_tensor_stage_status': [_i, _ip],
     'qg_set_host_direct': [_i],
     'qg_set_pageable_copy': [_i],
+    'qg_set_pool_guide_index_shift': [_i],
     'qg_gate_stats': [_i64p, _i64p, _i64p, _i],
     'qg_timing_enable': [_i],
     'qg_timing_read': [ctypes.c_char_p, _i64p, _dp, _i],

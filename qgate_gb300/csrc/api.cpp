@@ -129,7 +129,7 @@ struct Pool {
     unsigned long long *cdf = nullptr;  // fixed-point prefix sums, 2^-60 units
     unsigned long long total = 0;       // cdf[n - 1]
     unsigned *guide = nullptr;          // guide table (nullptr: plain search)
-    int guide_shift = 0;
+    int guide_shift = 0, guide_index_shift = 0;
     idx_t n = 0;
     std::vector<int> empty_pos;  // ascending
 };
@@ -139,6 +139,7 @@ struct Device {
     int dev = 0;
     cudaStream_t stream = nullptr;
     Arena arena;
+    int guide_index_shift = -1;    // pools' guide entries: -1 = automatic
     double *d_partials = nullptr;  // reduce_partials() + 8
     double *h_result = nullptr;    // pinned, 16 doubles
     static constexpr size_t kStageBytes = 64ull << 20;
@@ -1380,6 +1381,13 @@ int qg_tensor_stage_status(int reset, int *status) {
     QG_END
 }
 
+int qg_set_pool_guide_index_shift(int k) {
+    QG_BEGIN
+    if (k < -1 || k > 8) fail(QG_ERR_VALUE, "guide index shift must be in [-1, 8].");
+    dev().guide_index_shift = k;
+    QG_END
+}
+
 int qg_set_pageable_copy(int on) {
     QG_BEGIN
     Device &d = dev();
@@ -1872,14 +1880,18 @@ int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_t
     }
     unsigned long long total = 0;
     // Guide table: buckets of 2^(64 - n_lanes) CDF units, about 16 items each
-    // for a normalised state; entries cover totals up to (1 + 1/16) * 2^60,
-    // beyond the norm check's 1.05.
+    // for a normalised state (64 above 2^32 items, whose entries then hold
+    // the item index shifted right to fit 32 bits); entries cover totals up
+    // to (1 + 1/16) * 2^60, beyond the norm check's 1.05.
     PoolGuide guide{};
     void *guide_aux = nullptr;
     const unsigned kLongCap = 1u << 16;
     try {
-        if (n_lanes >= 12 && n_lanes <= 32) {
-            guide.shift = 64 - n_lanes;
+        if (n_lanes >= 12 && n_lanes <= 34) {
+            // 32-bit entries need index >> (lanes - 32) at least
+            const int ks = std::max(d.guide_index_shift, std::max(0, n_lanes - 32));
+            guide.shift = ks == 0 ? 64 - n_lanes : 66 - n_lanes;
+            guide.index_shift = ks;
             guide.nb = (((1ull << 60) + (1ull << 56)) >> guide.shift) + 2;
             guide.g = (unsigned *)d.arena.alloc(guide.nb * sizeof(unsigned));
             guide_aux = d.arena.alloc(16 + (size_t)kLongCap * sizeof(uint4));
@@ -1931,6 +1943,7 @@ int qg_qubits_states_getter_create_sampling_pool(qg_handle hg, const int *lane_t
     p->total = total;
     p->guide = guide.g;
     p->guide_shift = guide.shift;
+    p->guide_index_shift = guide.index_shift;
     p->n = n;
     for (int i = 0; i < n_empty; ++i) p->empty_pos.push_back(empty_lanes[i]);
     std::sort(p->empty_pos.begin(), p->empty_pos.end());
@@ -1959,7 +1972,8 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
         try {
             QG_CUDA(cudaMemcpyAsync(du, randnum, bytes, cudaMemcpyHostToDevice, d.stream));
             timed(d, "search", [&] {
-                launch_search(p->cdf, p->n, p->total, p->guide, p->guide_shift, du, dobs,
+                launch_search(p->cdf, p->n, p->total, p->guide, p->guide_shift,
+                              p->guide_index_shift, du, dobs,
                               n_samples, p->empty_pos.data(),
                               (int)p->empty_pos.size(), d.stream);
             });
@@ -1991,7 +2005,8 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
             host_copy(d.h_stage[0], randnum + b, cnt * 8);
             QG_CUDA(cudaMemcpyAsync(du, d.h_stage[0], cnt * 8, cudaMemcpyHostToDevice, d.stream));
             timed(d, "search", [&] {
-                launch_search(p->cdf, p->n, p->total, p->guide, p->guide_shift, du, dobs, cnt,
+                launch_search(p->cdf, p->n, p->total, p->guide, p->guide_shift,
+                              p->guide_index_shift, du, dobs, cnt,
                               p->empty_pos.data(),
                               (int)p->empty_pos.size(), d.stream);
             });

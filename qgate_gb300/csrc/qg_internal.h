@@ -349,7 +349,8 @@ void launch_convert_f64(int prec, void *dst, const double *src, idx_t n, cudaStr
 // of the total, which saturates at 2^64 - 1; pool_status reports a bounded
 // wait of the bulk-copy kernels that gave up.
 // The scan also fills the pool's guide table when g is set: g[b] = the first
-// i with cdf[i] > b * 2^shift for b < nb (nb must exceed (total - 1) >> shift),
+// i with cdf[i] > b * 2^shift, shifted right by index_shift, for b < nb (nb
+// must exceed (total - 1) >> shift),
 // with runs of more than 8 buckets per item passed through long_list (at most
 // long_cap entries; *long_count, zeroed by the caller, above long_cap means
 // the table is incomplete and must not be used).
@@ -357,6 +358,7 @@ struct PoolGuide {
     unsigned *g;
     unsigned long long nb;
     int shift;
+    int index_shift;  // entries hold item >> index_shift (lower bounds)
     unsigned *long_count;
     uint4 *long_list;
     unsigned long_cap;
@@ -373,8 +375,9 @@ const unsigned long long *launch_pool_cdf_prob(const double *prob, idx_t n,
 int pool_status(bool reset);
 // guide: the pool's table (nullptr: plain binary search over cdf).
 void launch_search(const unsigned long long *cdf, idx_t n, unsigned long long total,
-                   const unsigned *guide, int shift, const double *u, long long *obs,
-                   idx_t n_samples, const int *empty_pos, int n_empty, cudaStream_t stream);
+                   const unsigned *guide, int shift, int index_shift, const double *u,
+                   long long *obs, idx_t n_samples, const int *empty_pos, int n_empty,
+                   cudaStream_t stream);
 
 inline SetSlots make_set_slots(const int *rb, int rl, int m, int prec) {
     SetSlots ss;

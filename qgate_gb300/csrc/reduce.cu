@@ -103,11 +103,16 @@ k_prob_vec2_f32(const float4 *__restrict__ s, idx_t n_vec, PairIdx pi, double *p
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
-template <class R> __device__ __forceinline__ R parity_sign_r(idx_t b) {
-    return (__popcll((unsigned long long)b) & 1) ? R(-1) : R(1);
+// w with its sign flipped when the parity bit par is 1.
+__device__ __forceinline__ float sign_flip(float w, unsigned par) {
+    return __int_as_float(__float_as_int(w) ^ (int)(par << 31));
 }
+__device__ __forceinline__ double sign_flip(double w, unsigned par) {
+    return __longlong_as_double(__double_as_longlong(w) ^ (long long)((unsigned long long)par << 63));
+}
+__device__ __forceinline__ unsigned parity64(idx_t b) { return (unsigned)__popcll(b) & 1u; }
 
-// <psi|P|psi>, diagonal Pauli string (x_mask == 0).
+// <psi|P|psi>, diagonal Pauli string (x_mask == 0): sum of (-1)^parity(b & z) |psi[b]|^2.
 template <class R>
 __global__ void __launch_bounds__(kRedThreads)
 k_pauli_diag(const typename CT<R>::type *__restrict__ s, idx_t n, unsigned long long z_mask,
@@ -122,38 +127,34 @@ k_pauli_diag(const typename CT<R>::type *__restrict__ s, idx_t n, unsigned long 
         R part = 0;
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u)
-            part += parity_sign_r<R>((b + u * stride) & (idx_t)z_mask) * abs2r(v[u]);
+            part += sign_flip(abs2r(v[u]), parity64((b + u * stride) & (idx_t)z_mask));
         acc += (double)part;
     }
-    for (; b < n; b += stride)
-        acc += (double)(parity_sign_r<R>(b & (idx_t)z_mask) * abs2r(s[b]));
+    for (; b < n; b += stride) acc += (double)sign_flip(abs2r(s[b]), parity64(b & (idx_t)z_mask));
     acc = block_sum(acc);
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
-// <psi|P|psi> with x_mask != 0: pairs (b, b ^ x_mask), b with the highest
-// x bit clear; ny = number of Y factors (x & z).  With w = conj(psi[b^x]) psi[b]
-// and s1, s2 the Z-signs of b and b^x, the pair contributes
-// Re(i^ny (s1 w + s2 conj(w))).
+// <psi|P|psi> with x_mask != 0: pairs (b, b2 = b ^ x_mask), b with the highest
+// x bit clear; ny = number of Y factors (x & z).  With w = conj(psi[b2]) psi[b]
+// and s1, s2 the Z-signs of b and b2, the pair contributes
+// Re(i^ny (s1 w + s2 conj(w))) (qgate/model/pauli_gates_diagonalizer.py
+// gives the same operator as a basis change).  Since s2 = s1 (-1)^ny, that is
+// coef * s1 * (Re w for even ny, Im w for odd ny) with coef = 2, -2, -2, 2 for
+// ny mod 4 = 0..3: one parity per pair, applied as a sign flip, and coef
+// multiplies the block's partial (exactly).
 template <class R>
 __global__ void __launch_bounds__(kRedThreads)
 k_pauli_pair(const typename CT<R>::type *__restrict__ s, idx_t n_items, int hbit,
              unsigned long long x_mask, unsigned long long z_mask, int ny, double *partials) {
     typedef typename CT<R>::type C;
+    const bool odd = ny & 1;
     double acc = 0.;
     const idx_t stride = (idx_t)gridDim.x * blockDim.x;
     idx_t k = (idx_t)blockIdx.x * blockDim.x + threadIdx.x;
     auto term = [&](idx_t b, C p, C q) -> R {
-        const idx_t b2 = b ^ (idx_t)x_mask;
-        R wr = q.x * p.x + q.y * p.y;
-        R wi = q.x * p.y - q.y * p.x;
-        R s1 = parity_sign_r<R>(b & (idx_t)z_mask), s2 = parity_sign_r<R>(b2 & (idx_t)z_mask);
-        switch (ny & 3) {
-        case 0: return (s1 + s2) * wr;
-        case 1: return -(s1 - s2) * wi;
-        case 2: return -(s1 + s2) * wr;
-        default: return (s1 - s2) * wi;
-        }
+        const R w = odd ? q.x * p.y - q.y * p.x : q.x * p.x + q.y * p.y;
+        return sign_flip(w, parity64(b & (idx_t)z_mask));
     };
     for (; k + (kUnroll - 1) * stride < n_items; k += kUnroll * stride) {
         // all loads first: 2 x kUnroll amplitudes in flight per thread
@@ -175,7 +176,7 @@ k_pauli_pair(const typename CT<R>::type *__restrict__ s, idx_t n_items, int hbit
         acc += (double)term(b, s[b], s[b ^ (idx_t)x_mask]);
     }
     acc = block_sum(acc);
-    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc * ((ny + 1) & 2 ? -2. : 2.);
 }
 
 // ------------------------------------------------------------ gathers
@@ -434,13 +435,14 @@ __device__ __noinline__ void guide_mark_slow(const Guide gd, unsigned i, long lo
 }
 
 // Item i's bucket b after the previous item's bucket bp: usually equal (no
-// bucket starts here) or one more (one store).
+// bucket starts here) or one more (one store).  Entries hold i >> index_shift
+// (0 up to 2^32 items), a lower bound of the item.
 __device__ __forceinline__ void guide_mark(const Guide &gd, idx_t i, int bp, int b) {
     if (b == bp) return;
     if (b == bp + 1 && (unsigned)b < gd.nb)
-        gd.g[b] = (unsigned)i;
+        gd.g[b] = (unsigned)(i >> gd.index_shift);
     else
-        guide_mark_slow(gd, (unsigned)i, (long long)bp + 1, b);
+        guide_mark_slow(gd, (unsigned)(i >> gd.index_shift), (long long)bp + 1, b);
 }
 
 // Fills the long runs: every thread of the grid walks the list.
@@ -756,12 +758,12 @@ struct EmptyPos {
 
 // With a guide table, t = floor(u * T) < T lies in bucket b = t >> shift <=
 // bmax = (T - 1) >> shift; the answer is in [g[b], g[b + 1]] (g[b + 1] read
-// as n - 1 past bmax), where cdf[hi] > t holds, so a lower-bound search over
-// that range finds it.
+// as n - 1 past bmax; entries widened by the index shift), where cdf[hi] > t
+// holds, so a lower-bound search over that range finds it.
 __global__ void __launch_bounds__(256)
 k_search(const u64 *__restrict__ cdf, idx_t n, u64 total, const unsigned *__restrict__ guide,
-         int shift, const double *__restrict__ u, long long *__restrict__ obs, idx_t m,
-         EmptyPos ep) {
+         int shift, int index_shift, const double *__restrict__ u, long long *__restrict__ obs,
+         idx_t m, EmptyPos ep) {
     const idx_t stride = (idx_t)gridDim.x * blockDim.x;
     const u64 bmax = (total - 1) >> shift;
     for (idx_t i = (idx_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
@@ -772,8 +774,11 @@ k_search(const u64 *__restrict__ cdf, idx_t n, u64 total, const unsigned *__rest
         } else if (guide && x >= 0.) {
             const u64 t = fix_target(x, total);
             const u64 b = t >> shift;
-            lo = guide[b];
-            idx_t hi = b + 1 <= bmax ? (idx_t)guide[b + 1] : n - 1;
+            lo = (idx_t)guide[b] << index_shift;
+            idx_t hi = b + 1 <= bmax
+                           ? ((idx_t)guide[b + 1] << index_shift) + ((1LL << index_shift) - 1)
+                           : n - 1;
+            if (hi > n - 1) hi = n - 1;
             while (lo < hi) {
                 const idx_t mid = (lo + hi) >> 1;
                 if (cdf[mid] <= t)
@@ -1058,13 +1063,14 @@ int pool_status(bool reset) {
 }
 
 void launch_search(const unsigned long long *cdf, idx_t n, unsigned long long total,
-                   const unsigned *guide, int shift, const double *u, long long *obs,
-                   idx_t n_samples, const int *empty_pos, int n_empty, cudaStream_t stream) {
+                   const unsigned *guide, int shift, int index_shift, const double *u,
+                   long long *obs, idx_t n_samples, const int *empty_pos, int n_empty,
+                   cudaStream_t stream) {
     if (n_samples <= 0) return;
     EmptyPos ep;
     ep.n = n_empty;
     for (int i = 0; i < n_empty; ++i) ep.pos[i] = empty_pos[i];
-    k_search<<<sm_grid(n_samples, 256, 152 * 16), 256, 0, stream>>>(cdf, n, total, guide, shift, u, obs,
+    k_search<<<sm_grid(n_samples, 256, 152 * 16), 256, 0, stream>>>(cdf, n, total, guide, shift, index_shift, u, obs,
                                                                    n_samples, ep);
     QG_CUDA(cudaGetLastError());
 }

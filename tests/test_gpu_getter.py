@@ -268,6 +268,33 @@ def test_sampling_pool_guide_long_runs(rt, n, n_h, flips):
         assert np.all(got[u >= 1.] == (1 << n) - 1) and np.all(got[~(u >= 0.)] == 0)
 
 
+@pytest.mark.parametrize('k', [1, 3])
+def test_sampling_pool_shifted_guide_entries(rt, k):
+    """The guide layout of pools above 2^32 items (entries = item >> k,
+    buckets of ~64 items), forced on a 20-qubit random state and on a basis
+    state: samples equal the integer model exactly."""
+    from qgate_gb300 import _native as nat
+    n = 20
+    rng = np.random.default_rng(30 + k)
+    getter = rt.create_qubits_states_getter(np.float32)
+    nat.call('qg_set_pool_guide_index_shift', k)
+    try:
+        for ops in (random_ops(rng, n, 40, max_controls=1), [('g', 'X', (), False, 7, ())]):
+            qs = new_state(rt, n, np.float32)
+            apply_ops(qs, ops)
+            lanes = [(qs, [Lane(l, l) for l in range(n)])]
+            probs = np.empty(1 << n, np.float32)
+            getter.get_states(probs, 0, abs2, lanes, [], 1 << n, 0, 1)
+            u = np.concatenate([rng.random(50000), EDGE_U])
+            pool = getter.create_sampling_pool(list(range(n)), n, 0, lanes, [])
+            got = np.asarray(pool.sample(len(u), u).intarray)
+            pool.delete()
+            qs.delete()
+            assert np.array_equal(got, _fixed_point_samples(probs, u))
+    finally:
+        nat.call('qg_set_pool_guide_index_shift', -1)
+
+
 def test_sampling_pool_rejects_unnormalised_state(rt):
     """|sum - 1| > 0.05 raises, as CPUSamplingPool does
     (qgate/simulator/src/CPUSamplingPool.cpp:31-32)."""
