@@ -116,6 +116,32 @@ int qg_qubit_processor_apply_controlled_gate(qg_handle proc, const double *mat,
                                              qg_handle qstates, const int *local_control_lanes,
                                              int n_controls, int local_target_lane);
 
+/* Extension: compiled circuits.  The reference front-end hands a circuit to
+ * the runtime one gate per call (qgate/simulator/rop_executor.py:28-34 via
+ * qgate/simulator/model_executor.py:151-166); a compiled circuit takes the
+ * whole gate list once and applies it in one call.
+ *   qg_circuit_new: n_gates gates; gate i has target lane targets[i], control
+ *   lanes ctrl_lanes[ctrl_offsets[i] .. ctrl_offsets[i+1]) (ctrl_offsets has
+ *   n_gates + 1 entries) and the 2x2 complex128 matrix matrices[8i .. 8i+8)
+ *   (row-major, interleaved re/im; adjoints already applied).  Lanes are
+ *   checked as apply_controlled_gate checks them (range, no overlap).
+ *   qg_circuit_run: applies the gates to qstates (same precision, at least as
+ *   many lanes as the circuit uses) exactly as the same sequence of
+ *   apply_gate / apply_controlled_gate calls would.
+ *   qg_circuit_set_graph: 1 = graph replay: the first run on a states buffer
+ *   plans the stages and captures their launches into a CUDA graph, later
+ *   runs on the same buffer (same lane count, unchanged fusion settings)
+ *   replay it without host planning; a different buffer, lane count or any
+ *   qg_set_fusion* / tensor / pipelining change re-captures.  The circuit
+ *   owns the graph and the tensor stages' operands (a few MB).
+ *   qg_circuit_stats: whether a graph is captured and its HBM passes. */
+int qg_circuit_new(int prec, int n_gates, const int *targets, const int *ctrl_offsets,
+                   const int *ctrl_lanes, const double *matrices, qg_handle *out);
+int qg_circuit_set_graph(qg_handle circuit, int on);
+int qg_circuit_run(qg_handle circuit, qg_handle qstates);
+int qg_circuit_stats(qg_handle circuit, int *captured, int64_t *passes);
+int qg_circuit_delete(qg_handle circuit);
+
 /* Extension: dense 2^k x 2^k complex128 matrix (row-major, interleaved re/im)
  * on k target lanes (targets[0] = least significant matrix bit), optionally
  * controlled.  k <= 6.  Replaces the reference's expansions of multi-qubit

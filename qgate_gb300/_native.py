@@ -50,6 +50,11 @@ SIGNATURES = {
     # per-gate entry points take raw addresses (ints) for speed
     'qg_qubit_processor_apply_gate': [_h, _vp, _h, _i],
     'qg_qubit_processor_apply_controlled_gate': [_h, _vp, _h, _vp, _i, _i],
+    'qg_circuit_new': [_i, _i, _ip, _ip, _ip, _dp, _hp],
+    'qg_circuit_set_graph': [_h, _i],
+    'qg_circuit_run': [_h, _h],
+    'qg_circuit_stats': [_h, _ip, _i64p],
+    'qg_circuit_delete': [_h],
     'qg_qubit_processor_apply_multi': [_h, _dp, _h, _ip, _i, _ip, _i],
     'qg_qubit_processor_calc_pauli_expectation': [_h, _h, _u64, _u64, _dp],
     'qg_qubit_processor_calc_norm': [_h, _h, _dp],

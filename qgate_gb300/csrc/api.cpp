@@ -134,12 +134,36 @@ struct Pool {
     std::vector<int> empty_pos;  // ascending
 };
 
+// A compiled circuit: a gate list handed over once and applied in one call.
+// With graph replay on, the first run on a states buffer plans and launches
+// the gates under stream capture; later runs on the same buffer (same lanes,
+// same fusion settings) replay that CUDA graph without host planning.  The
+// tensor stages' block operands of a captured graph live in chunks the
+// circuit owns (pinned staging + device copy), so replays re-read them.
+struct Circuit {
+    int prec;
+    int min_lanes = 0;
+    std::vector<PendingGate> gates;
+    bool graph = false;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void *state = nullptr;  // what the graph was captured for
+    int n_lanes = -1;
+    unsigned version = 0;
+    long long passes = 0, bytes = 0;
+    static constexpr size_t kChunkBytes = 8ull << 20;
+    std::vector<std::pair<unsigned short *, unsigned short *>> chunks;
+    size_t chunk_off = 0;
+};
+
 struct Device {
     bool initialized = false;
     int dev = 0;
     cudaStream_t stream = nullptr;
     Arena arena;
     int guide_index_shift = -1;    // pools' guide entries: -1 = automatic
+    unsigned settings_version = 1;  // bumped by every change of the fusion settings
+    struct Circuit *capturing = nullptr;  // set while a compiled circuit is captured
     double *d_partials = nullptr;  // reduce_partials() + 8
     double *h_result = nullptr;    // pinned, 16 doubles
     static constexpr size_t kStageBytes = 64ull << 20;
@@ -187,6 +211,7 @@ struct Device {
     std::unordered_set<Processor *> procs;
     std::unordered_set<Getter *> getters;
     std::unordered_set<Pool *> pools;
+    std::unordered_set<struct Circuit *> circuits;
     std::recursive_mutex mu;
 };
 
@@ -499,17 +524,36 @@ static void run_tstage(Device &d, States *s, const TileLanes &tl,
     for (size_t b0 = 0; b0 < blocks.size(); b0 += per_launch) {
         const int nb = (int)std::min<size_t>(per_launch, blocks.size() - b0);
         const size_t bytes = nb * kBlockHalves * sizeof(unsigned short);
-        if (d.bring_off + bytes > Device::kBRingBytes) {
-            QG_CUDA(cudaStreamSynchronize(d.stream));  // the staging is reused
-            d.bring_off = 0;
+        unsigned short *hb, *db;
+        if (d.capturing) {
+            // operands a captured graph re-reads: chunks owned by the circuit
+            Circuit *c = d.capturing;
+            if (c->chunks.empty() || c->chunk_off + bytes > Circuit::kChunkBytes) {
+                unsigned short *h = nullptr, *dv = nullptr;
+                QG_CUDA(cudaMallocHost(&h, Circuit::kChunkBytes));
+                if (cudaMalloc(&dv, Circuit::kChunkBytes) != cudaSuccess) {
+                    cudaFreeHost(h);
+                    fail(QG_ERR_NOMEM, "circuit operand chunk: device allocation failed.");
+                }
+                c->chunks.emplace_back(h, dv);
+                c->chunk_off = 0;
+            }
+            hb = c->chunks.back().first + c->chunk_off / sizeof(unsigned short);
+            db = c->chunks.back().second + c->chunk_off / sizeof(unsigned short);
+            c->chunk_off += bytes;
+        } else {
+            if (d.bring_off + bytes > Device::kBRingBytes) {
+                QG_CUDA(cudaStreamSynchronize(d.stream));  // the staging is reused
+                d.bring_off = 0;
+            }
+            hb = d.h_bring + d.bring_off / sizeof(unsigned short);
+            db = d.d_bring + d.bring_off / sizeof(unsigned short);
+            d.bring_off += bytes;
         }
-        unsigned short *hb = d.h_bring + d.bring_off / sizeof(unsigned short);
-        unsigned short *db = d.d_bring + d.bring_off / sizeof(unsigned short);
         static TcStageDesc desc;
         tc_plan_launch(tl, n, blocks, b0, nb, desc, hb);
         desc.bmats = db;
         QG_CUDA(cudaMemcpyAsync(db, hb, bytes, cudaMemcpyHostToDevice, d.stream));
-        d.bring_off += bytes;
         timed(d, "tstage", [&] { launch_tstage(s->d, desc, d.stream, d.pipelined); });
         d.n_passes += 1;
         d.n_bytes += 2 * ((long long)1 << n) * (long long)complex_size(s->prec);
@@ -1256,6 +1300,167 @@ int qg_qubit_processor_apply_controlled_gate(qg_handle hp, const double *mat, qg
     QG_END
 }
 
+// ------------------------------------------------------------ compiled circuits
+
+static void drop_graph(Device &d, Circuit *c) {
+    if (c->exec || !c->chunks.empty()) QG_CUDA(cudaStreamSynchronize(d.stream));
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    if (c->g) cudaGraphDestroy(c->g);
+    for (auto &ch : c->chunks) {
+        cudaFreeHost(ch.first);
+        cudaFree(ch.second);
+    }
+    c->chunks.clear();
+    c->chunk_off = 0;
+    c->exec = nullptr;
+    c->g = nullptr;
+    c->state = nullptr;
+    c->n_lanes = -1;
+}
+
+// Plans the circuit's gates on s under stream capture (nothing runs) and
+// instantiates the graph.  The states object's queue must be empty.
+static void capture_circuit(Device &d, Circuit *c, States *s) {
+    const bool timing = d.timing;
+    const long long p0 = d.n_passes, b0 = d.n_bytes;
+    d.timing = false;
+    d.capturing = c;
+    cudaGraph_t graph = nullptr;
+    auto restore = [&] {
+        d.capturing = nullptr;
+        d.timing = timing;
+        d.n_passes = p0;
+        d.n_bytes = b0;
+        s->pending.clear();
+    };
+    QG_CUDA(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeRelaxed));
+    try {
+        s->pending = c->gates;
+        flush(s);
+    } catch (...) {
+        cudaStreamEndCapture(d.stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        restore();
+        throw;
+    }
+    const cudaError_t ec = cudaStreamEndCapture(d.stream, &graph);
+    c->passes = d.n_passes - p0;
+    c->bytes = d.n_bytes - b0;
+    restore();
+    cuda_check(ec, "cudaStreamEndCapture");
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    if (ei != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        cuda_check(ei, "cudaGraphInstantiate");
+    }
+    c->g = graph;
+    c->exec = exec;
+    c->state = s->d;
+    c->n_lanes = s->n_lanes;
+    c->version = d.settings_version;
+}
+
+int qg_circuit_new(int prec, int n_gates, const int *targets, const int *ctrl_offsets,
+                   const int *ctrl_lanes, const double *matrices, qg_handle *out) {
+    QG_BEGIN
+    check_prec(prec);
+    if (n_gates < 0) fail(QG_ERR_VALUE, "negative gate count.");
+    if (n_gates > 0 && (!targets || !ctrl_offsets || !matrices))
+        fail(QG_ERR_VALUE, "null gate arrays.");
+    Circuit *c = new Circuit();
+    c->prec = prec;
+    try {
+        c->gates.reserve(n_gates);
+        for (int i = 0; i < n_gates; ++i) {
+            PendingGate g;
+            g.target = targets[i];
+            if (g.target < 0 || g.target >= kMaxLanes)
+                fail(QG_ERR_VALUE, "gate %d: target lane %d out of range.", i, g.target);
+            unsigned long long seen = 1ULL << g.target;
+            c->min_lanes = std::max(c->min_lanes, g.target + 1);
+            if (ctrl_offsets[i + 1] < ctrl_offsets[i] || (ctrl_offsets[i + 1] > ctrl_offsets[i] && !ctrl_lanes))
+                fail(QG_ERR_VALUE, "gate %d: bad control offsets.", i);
+            for (int k = ctrl_offsets[i]; k < ctrl_offsets[i + 1]; ++k) {
+                const int cl = ctrl_lanes[k];
+                if (cl < 0 || cl >= kMaxLanes)
+                    fail(QG_ERR_VALUE, "gate %d: control lane %d out of range.", i, cl);
+                if (seen & (1ULL << cl)) fail(QG_ERR_RUNTIME, "control and operand overlapped.");
+                seen |= 1ULL << cl;
+                g.controls.push_back(cl);
+                c->min_lanes = std::max(c->min_lanes, cl + 1);
+            }
+            memcpy(g.m.v, matrices + 8 * (size_t)i, sizeof(g.m.v));
+            g.diag = is_diag(g.m);
+            c->gates.push_back(std::move(g));
+        }
+    } catch (...) {
+        delete c;
+        throw;
+    }
+    g_dev.circuits.insert(c);
+    *out = (qg_handle)c;
+    QG_END
+}
+
+int qg_circuit_set_graph(qg_handle hc, int on) {
+    QG_BEGIN
+    Circuit *c = lookup(g_dev.circuits, hc, "circuit");
+    if (!on && c->graph) drop_graph(dev(), c);
+    c->graph = on != 0;
+    QG_END
+}
+
+int qg_circuit_run(qg_handle hc, qg_handle hs) {
+    QG_BEGIN
+    Circuit *c = lookup(g_dev.circuits, hc, "circuit");
+    States *s = get_alloc_states(hs);
+    if (s->prec != c->prec) fail(QG_ERR_VALUE, "precision mismatch between circuit and states.");
+    if (s->n_lanes < c->min_lanes)
+        fail(QG_ERR_VALUE, "circuit uses %d lanes, the states object has %d.", c->min_lanes,
+             s->n_lanes);
+    Device &d = dev();
+    if (c->gates.empty()) {
+        t_last_error.clear();
+        return QG_OK;
+    }
+    if (!c->graph) {
+        for (const auto &g : c->gates) {
+            s->pending.push_back(g);
+            stream_flush(s);
+        }
+        d.n_gates += (long long)c->gates.size();
+    } else {
+        flush(s);  // earlier gates of this states object run first
+        if (c->exec && (c->state != s->d || c->n_lanes != s->n_lanes ||
+                        c->version != d.settings_version))
+            drop_graph(d, c);
+        if (!c->exec) capture_circuit(d, c, s);
+        QG_CUDA(cudaGraphLaunch(c->exec, d.stream));
+        d.n_gates += (long long)c->gates.size();
+        d.n_passes += c->passes;
+        d.n_bytes += c->bytes;
+    }
+    QG_END
+}
+
+int qg_circuit_stats(qg_handle hc, int *captured, int64_t *passes) {
+    QG_BEGIN
+    Circuit *c = lookup(g_dev.circuits, hc, "circuit");
+    *captured = c->exec != nullptr;
+    *passes = c->passes;
+    QG_END
+}
+
+int qg_circuit_delete(qg_handle hc) {
+    QG_BEGIN
+    Circuit *c = lookup(g_dev.circuits, hc, "circuit");
+    drop_graph(dev(), c);
+    g_dev.circuits.erase(c);
+    delete c;
+    QG_END
+}
+
 int qg_qubit_processor_apply_multi(qg_handle hp, const double *mat, qg_handle hs,
                                    const int *targets, int n_targets, const int *ctrl,
                                    int n_ctrl) {
@@ -1336,6 +1541,7 @@ int qg_set_fusion(int max_tile_lanes) {
     if (max_tile_lanes < 0 || max_tile_lanes > kMaxTileLanes)
         fail(QG_ERR_VALUE, "max_tile_lanes must be in [0, %d].", kMaxTileLanes);
     flush_all();
+    g_dev.settings_version += 1;  // compiled circuits re-plan
     if (max_tile_lanes == 0) {
         g_dev.tile_lanes[kFP32] = 12;
         g_dev.tile_lanes[kFP64] = 12;
@@ -1359,6 +1565,7 @@ int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budge
     if (reg_lanes < 3 || reg_lanes > kMaxRegLanes) fail(QG_ERR_VALUE, "reg_lanes must be in [3, 5].");
     if (cost_budget < 0) fail(QG_ERR_VALUE, "cost_budget must be >= 0.");
     flush_all();
+    g_dev.settings_version += 1;  // compiled circuits re-plan
     g_dev.tile_lanes[prec] = tile_lanes;
     g_dev.reg_lanes[prec] = reg_lanes;
     g_dev.cost_budget[prec] = cost_budget;
@@ -1368,6 +1575,7 @@ int qg_set_fusion_params(int prec, int tile_lanes, int reg_lanes, int cost_budge
 int qg_set_tensor_blocks(int on) {
     QG_BEGIN
     flush_all();
+    g_dev.settings_version += 1;  // compiled circuits re-plan
     g_dev.tensor_blocks = on != 0;
     QG_END
 }
@@ -1409,6 +1617,7 @@ int qg_set_host_direct(int on) {
 int qg_set_stage_pipelining(int on) {
     QG_BEGIN
     flush_all();
+    g_dev.settings_version += 1;  // compiled circuits re-plan
     g_dev.pipelined = on != 0;
     QG_END
 }
