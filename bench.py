@@ -373,6 +373,10 @@ def run_gb300(args):
     if rank == 0 and not args.no_e2e:
         kernels = observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2)
 
+    compiled = None
+    if rank == 0 and not args.no_compiled:
+        compiled = run_compiled(args, rt, nat)
+
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch(args, nat)
@@ -418,6 +422,7 @@ def run_gb300(args):
                 'gates_per_s': stats['gates'] / args.steps / (t_max / args.steps / 1e3)}),
             'roofline': roofline,
             'observation_kernels': kernels,
+            'compiled': compiled,
             'accuracy': accuracy,
             'adjoint': adjoint,
             'batch': batch,
@@ -510,6 +515,65 @@ def qft_ops(n, seed):
         for j in range(i + 1, n):
             ops.append(('U1', (math.pi / (1 << (j - i)),), i, (j,)))
     return ops
+
+
+def run_compiled(args, rt, nat):
+    """Per-run latency of whole circuits through the plugin API with one call
+    per gate (the reference front-end's pattern), against `CompiledCircuit`
+    (the gate table in one call) and its CUDA-graph replay: the 20-qubit QFT
+    of BASELINE config 0 (complex128 as specified, and complex64, where the
+    device work is small and the host's share shows; X preparation from
+    default_rng(0)) and the headline random circuit (complex64).  Wall time from reset to a
+    synchronised state, median of the repeats after one warm-up run (which
+    plans, and for the graph captures)."""
+    from qgate_gb300.circuit import gate_type
+    from qgate_gb300.compiled import CompiledCircuit
+    out = {}
+    cases = [('qft_20q_c128', 20, qft_ops(20, 0), np.float64, 20),
+             ('qft_20q_c64', 20, qft_ops(20, 0), np.float32, 20),
+             ('random_%dq_c64' % args.qubits, args.qubits, circuit(args.qubits, args.depth),
+              np.float32, 3)]
+    for label, n, ops, dtype, reps in cases:
+        gts = [(gate_type(nm, *a), False, t, list(c)) for nm, a, t, c in ops]
+        qs = rt.create_qubit_states(dtype)
+        proc = qs.processor
+        proc.initialize_qubit_states(qs, n)
+
+        def per_gate():
+            proc.reset_qubit_states(qs)
+            for gt, adj, t, c in gts:
+                if c:
+                    proc.apply_controlled_gate(gt, adj, qs, c, t)
+                else:
+                    proc.apply_gate(gt, adj, qs, t)
+            proc.synchronize()
+
+        def median_ms(f):
+            f()
+            ts = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                f()
+                ts.append(time.perf_counter() - t0)
+            return float(np.median(ts)) * 1e3
+
+        res = {'qubits': n, 'gates': len(gts), 'dtype': 'c128' if dtype == np.float64 else 'c64',
+               'per_gate_call_ms': median_ms(per_gate)}
+        for graph in (False, True):
+            circ = CompiledCircuit(dtype, gts, graph=graph)
+
+            def run():
+                proc.reset_qubit_states(qs)
+                circ.run(qs)
+                proc.synchronize()
+
+            res['graph_replay_ms' if graph else 'compiled_call_ms'] = median_ms(run)
+            if graph:
+                res['graph_passes'] = circ.stats()[1]
+            circ.delete()
+        qs.delete()
+        out[label] = res
+    return out
 
 
 def run_c4(args, rt, nat):
@@ -740,6 +804,7 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
+    ap.add_argument('--no-compiled', action='store_true')
     ap.add_argument('--c4', action='store_true', help='also run the 33/34-qubit large states')
     ap.add_argument('--c4-random-qubits', type=int, default=33)
     ap.add_argument('--c4-qft-qubits', type=int, default=34)
