@@ -177,11 +177,18 @@ def state_accuracy(rt, qs, gts, n, torch):
     pd = qd.processor
     pd.initialize_qubit_states(qd, n)
     pd.reset_qubit_states(qd)
+    pd.synchronize()
+    nat = sys.modules['qgate_gb300._native']
+    nat.gate_stats(reset=True)
+    t0 = time.perf_counter()
     for gt, t, c in gts:
         if c:
             pd.apply_controlled_gate(gt, False, qd, c, t)
         else:
             pd.apply_gate(gt, False, qd, t)
+    pd.synchronize()
+    c128_ms = (time.perf_counter() - t0) * 1e3
+    st = nat.gate_stats(reset=True)
     ref = qd.get_raw()
     qd.delete()
     got = qs.get_raw()
@@ -195,7 +202,11 @@ def state_accuracy(rt, qs, gts, n, torch):
         ov += torch.vdot(a, b).item()
         perr = max(perr, (a.abs() ** 2 - b.abs() ** 2).abs().max().item())
     return {'reference': 'the same circuit in complex128 (engine, CUDA-core FP64)',
-            'fidelity_err': abs(1. - abs(ov)), 'max_prob_err': perr, 'norm_c64': norm32}
+            'fidelity_err': abs(1. - abs(ov)), 'max_prob_err': perr, 'norm_c64': norm32,
+            'c128_circuit_ms': c128_ms, 'c128_passes': st['passes'],
+            'c128_hbm_gbs_actual': st['bytes'] / (c128_ms / 1e3) / 1e9,
+            'c128_note': 'complex128 stages are bound by GB300\'s FP64 rate (~2 FP64 '
+                         'operations per clock per SM), not by HBM'}
 
 
 def cpu_port_gate_rate(n, ops, cs, budget_s):
