@@ -170,8 +170,8 @@ def cpu_model():
 def state_accuracy(rt, qs, gts, n, torch):
     """Fidelity error |1 - |<psi128|psi64>||, max |p64 - p128| and the
     complex64 norm of the benchmark circuit's final state (`qs`, complex64)
-    against the same circuit run in complex128 by the engine (CUDA-core
-    FP64 kernels).  Both states are copied to the host; the overlap is summed
+    against the same circuit run in complex128 by the engine (FP64 state,
+    double-float register arithmetic), whose time is reported too.  Both states are copied to the host; the overlap is summed
     in FP64 in slices."""
     qd = rt.create_qubit_states(np.float64)
     pd = qd.processor
@@ -201,12 +201,14 @@ def state_accuracy(rt, qs, gts, n, torch):
         b = torch.from_numpy(got[i:i + step]).to(torch.complex128)
         ov += torch.vdot(a, b).item()
         perr = max(perr, (a.abs() ** 2 - b.abs() ** 2).abs().max().item())
-    return {'reference': 'the same circuit in complex128 (engine, CUDA-core FP64)',
+    return {'reference': 'the same circuit in complex128 (engine: FP64 state, double-float '
+                         'register arithmetic)',
             'fidelity_err': abs(1. - abs(ov)), 'max_prob_err': perr, 'norm_c64': norm32,
             'c128_circuit_ms': c128_ms, 'c128_passes': st['passes'],
             'c128_hbm_gbs_actual': st['bytes'] / (c128_ms / 1e3) / 1e9,
-            'c128_note': 'complex128 stages are bound by GB300\'s FP64 rate (~2 FP64 '
-                         'operations per clock per SM), not by HBM'}
+            'c128_note': 'complex128 stages compute in double-float on the FP32 pipes '
+                         '(GB300 runs ~2 FP64 operations per clock per SM); they stay '
+                         'arithmetic-bound, not HBM-bound'}
 
 
 def cpu_port_gate_rate(n, ops, cs, budget_s):

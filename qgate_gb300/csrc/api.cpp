@@ -173,7 +173,7 @@ struct Device {
     // shared-memory tile, lanes per thread's registers, per-amplitude cost
     // budget of a stage (0 = unlimited).
     int tile_lanes[3] = {0, 12, 12};
-    int reg_lanes[3] = {0, 4, 4};
+    int reg_lanes[3] = {0, 3, 4};  // complex128 (double-float registers): 3
     int cost_budget[3] = {0, 0, 0};
     bool pipelined = false;  // persistent double-buffered stage kernel (opt-in)
     // Kernels may write results straight into the caller's (pageable) host
@@ -560,6 +560,21 @@ static void run_tstage(Device &d, States *s, const TileLanes &tl,
     }
 }
 
+// complex128 register stages compute in double-float: each FP64 matrix
+// entry of an op is packed as its (h, l) FP32 pair, h = fl32(v), l =
+// fl32(v - h), in the entry's own 8-byte slot.
+static void pack_double_float(RStageDesc<double> &desc) {
+    for (int i = 0; i < desc.nops; ++i) {
+        RegOp<double> &o = desc.ops[i];
+        if (o.kind == kOpTranspose || o.kind == kOpSwapX) continue;
+        for (int k = 0; k < 8; ++k) {
+            const double v = o.m[k];
+            const float hl[2] = {(float)v, (float)(v - (double)(float)v)};
+            memcpy(&o.m[k], hl, sizeof(hl));
+        }
+    }
+}
+
 static void run_stage(Device &d, States *s, unsigned long long S,
                       const std::vector<const PendingGate *> &gates) {
     const int n = s->n_lanes;
@@ -588,7 +603,10 @@ static void run_stage(Device &d, States *s, unsigned long long S,
     } else {
         static RStageDesc<double> desc;
         ok = schedule_rstage(gates, tl, n, rl, desc);
-        if (ok) timed(d, "stage", [&] { launch_rstage_f64(s->d, desc, d.stream, d.pipelined); });
+        if (ok) {
+            pack_double_float(desc);
+            timed(d, "stage", [&] { launch_rstage_f64(s->d, desc, d.stream, d.pipelined); });
+        }
     }
     if (!ok) {
         // Program too long for one descriptor: split the stage.
@@ -1546,7 +1564,7 @@ int qg_set_fusion(int max_tile_lanes) {
         g_dev.tile_lanes[kFP32] = 12;
         g_dev.tile_lanes[kFP64] = 12;
         g_dev.reg_lanes[kFP32] = 4;
-        g_dev.reg_lanes[kFP64] = 4;
+        g_dev.reg_lanes[kFP64] = 3;
         g_dev.cost_budget[kFP32] = 0;
         g_dev.cost_budget[kFP64] = 0;
         g_dev.tensor_blocks = true;

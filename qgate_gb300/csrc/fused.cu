@@ -97,6 +97,63 @@ k_stage(typename CT<R>::type *__restrict__ s, const __grid_constant__ StageDesc 
 
 // ------------------------------------------------------------ register-resident stage
 
+// Runs a stage program on the staged tile sm.  Registers hold the register
+// arithmetic's type (FP32 complex for complex64, double-float for
+// complex128): the first register load converts from the tile, later
+// transposes move that type through shared memory unchanged.  Leaves the
+// registers and their slots (P0, q) for the caller's final store.
+template <class R, int RL, int TL>
+__device__ __forceinline__ void run_program(typename CT<R>::type *sm, const RegOp<R> *sops,
+                                            const SetSlots *sset, int nops, unsigned tid,
+                                            typename RegArith<R>::T (&a)[1 << RL], unsigned &P0,
+                                            unsigned (&q)[RL]) {
+    typedef RegArith<R> RA;
+    typedef typename RA::T RT;
+    constexpr int NR = 1 << RL;
+    RT *smr = (RT *)sm;
+    unsigned e0 = 0;
+    for (int oi = 0; oi < nops; ++oi) {
+        const RegOp<R> o = sops[oi];
+        if (o.kind == kOpTranspose) {
+            if (oi > 0) {
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < NR; ++j) smr[reg_slot<RL>(P0, q, j)] = a[j];
+                __syncthreads();
+            }
+            const SetSlots &ss = sset[o.reg];
+            P0 = (unsigned)ss.lo[tid & 31u] ^ (unsigned)ss.hi[tid >> 5];
+            e0 = Swz<R>::f(P0);  // the swizzle is an involution
+#pragma unroll
+            for (int k = 0; k < RL; ++k) q[k] = ss.q[k];
+            if (oi == 0) {
+#pragma unroll
+                for (int j = 0; j < NR; ++j) a[j] = RA::from_tile(sm[reg_slot<RL>(P0, q, j)]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < NR; ++j) a[j] = smr[reg_slot<RL>(P0, q, j)];
+            }
+            continue;
+        }
+        if ((e0 & o.tmask) != o.tmask) continue;
+        if (o.kind == kOpGate) {
+            const Mat2C<RT> mm = {RA::entry(o.m, 0), RA::entry(o.m, 1), RA::entry(o.m, 2),
+                                  RA::entry(o.m, 3)};
+            QG_REG_DISPATCH(reg_gate_c, o.reg, a, mm, (unsigned)o.jmask);
+        } else if (o.kind == kOpSwapX) {
+            QG_REG_DISPATCH(reg_swap, o.reg, a, (unsigned)o.jmask);
+        } else if (o.kind == kOpDiagReg) {
+            const RT d0 = RA::entry(o.m, 0), d1 = RA::entry(o.m, 3);
+            QG_REG_DISPATCH(reg_diag, o.reg, a, d0, d1, (unsigned)o.jmask);
+        } else {  // kOpDiagThread
+            const RT ph = (e0 & o.tbit) ? RA::entry(o.m, 3) : RA::entry(o.m, 0);
+#pragma unroll
+            for (int j = 0; j < NR; ++j)
+                if ((j & o.jmask) == o.jmask) a[j] = cmul(ph, a[j]);
+        }
+    }
+}
+
 // One CTA per tile of 2^m amplitudes, 2^(m-rl) threads, 2^rl amplitudes per
 // thread.  The stage program (ops, register sets, global offsets) is first
 // copied from the kernel parameters to shared memory, so that every thread
@@ -145,55 +202,16 @@ k_rstage(typename CT<R>::type *__restrict__ s, const __grid_constant__ RStageDes
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
 
-    C a[NR];
-    unsigned e0 = 0, P0 = 0;
+    typename RegArith<R>::T a[NR];
+    unsigned P0 = 0;
     unsigned q[RL];
 #pragma unroll
     for (int k = 0; k < RL; ++k) q[k] = 0;
-
-    const int nops = d.nops;
-    for (int oi = 0; oi < nops; ++oi) {
-        const Op o = sops[oi];
-        if (o.kind == kOpTranspose) {
-            if (oi > 0) {
-                __syncthreads();
-#pragma unroll
-                for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
-                __syncthreads();
-            }
-            const SetSlots &ss = sset[o.reg];
-            P0 = (unsigned)ss.lo[tid & 31u] ^ (unsigned)ss.hi[tid >> 5];
-            e0 = Swz<R>::f(P0);  // the swizzle is an involution
-#pragma unroll
-            for (int k = 0; k < RL; ++k) q[k] = ss.q[k];
-#pragma unroll
-            for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
-            continue;
-        }
-        if ((e0 & o.tmask) != o.tmask) continue;
-        if (o.kind == kOpGate) {
-            MatR<R> mm;
-            mm.m00 = cmk<C>(o.m[0], o.m[1]);
-            mm.m01 = cmk<C>(o.m[2], o.m[3]);
-            mm.m10 = cmk<C>(o.m[4], o.m[5]);
-            mm.m11 = cmk<C>(o.m[6], o.m[7]);
-            QG_REG_DISPATCH(reg_gate, o.reg, a, mm, (unsigned)o.jmask);
-        } else if (o.kind == kOpSwapX) {
-            QG_REG_DISPATCH(reg_swap, o.reg, a, (unsigned)o.jmask);
-        } else if (o.kind == kOpDiagReg) {
-            C d0 = cmk<C>(o.m[0], o.m[1]), d1 = cmk<C>(o.m[6], o.m[7]);
-            QG_REG_DISPATCH(reg_diag, o.reg, a, d0, d1, (unsigned)o.jmask);
-        } else {  // kOpDiagThread
-            C ph = (e0 & o.tbit) ? cmk<C>(o.m[6], o.m[7]) : cmk<C>(o.m[0], o.m[1]);
-#pragma unroll
-            for (int j = 0; j < NR; ++j)
-                if ((j & o.jmask) == o.jmask) a[j] = cmul(ph, a[j]);
-        }
-    }
+    run_program<R, RL, TL>(sm, sops, sset, d.nops, tid, a, P0, q);
 
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+    for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = RegArith<R>::to_tile(a[j]);
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < NR; ++i) gp[sdep[i]] = sm[pt ^ Swz<R>::f((unsigned)i << t)];
@@ -260,52 +278,15 @@ k_rstage_pipe(typename CT<R>::type *__restrict__ s, const __grid_constant__ RSta
         }
         __syncthreads();
 
-        C a[NR];
-        unsigned e0 = 0, P0 = 0;
+        typename RegArith<R>::T a[NR];
+        unsigned P0 = 0;
         unsigned q[RL];
 #pragma unroll
         for (int kk = 0; kk < RL; ++kk) q[kk] = 0;
-        for (int oi = 0; oi < nops; ++oi) {
-            const Op o = sops[oi];
-            if (o.kind == kOpTranspose) {
-                if (oi > 0) {
-                    __syncthreads();
-#pragma unroll
-                    for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
-                    __syncthreads();
-                }
-                const SetSlots &ss = sset[o.reg];
-                P0 = (unsigned)ss.lo[tid & 31u] ^ (unsigned)ss.hi[tid >> 5];
-                e0 = Swz<R>::f(P0);
-#pragma unroll
-                for (int kk = 0; kk < RL; ++kk) q[kk] = ss.q[kk];
-#pragma unroll
-                for (int j = 0; j < NR; ++j) a[j] = sm[reg_slot<RL>(P0, q, j)];
-                continue;
-            }
-            if ((e0 & o.tmask) != o.tmask) continue;
-            if (o.kind == kOpGate) {
-                MatR<R> mm;
-                mm.m00 = cmk<C>(o.m[0], o.m[1]);
-                mm.m01 = cmk<C>(o.m[2], o.m[3]);
-                mm.m10 = cmk<C>(o.m[4], o.m[5]);
-                mm.m11 = cmk<C>(o.m[6], o.m[7]);
-                QG_REG_DISPATCH(reg_gate, o.reg, a, mm, (unsigned)o.jmask);
-            } else if (o.kind == kOpSwapX) {
-                QG_REG_DISPATCH(reg_swap, o.reg, a, (unsigned)o.jmask);
-            } else if (o.kind == kOpDiagReg) {
-                C d0 = cmk<C>(o.m[0], o.m[1]), d1 = cmk<C>(o.m[6], o.m[7]);
-                QG_REG_DISPATCH(reg_diag, o.reg, a, d0, d1, (unsigned)o.jmask);
-            } else {
-                C ph = (e0 & o.tbit) ? cmk<C>(o.m[6], o.m[7]) : cmk<C>(o.m[0], o.m[1]);
-#pragma unroll
-                for (int j = 0; j < NR; ++j)
-                    if ((j & o.jmask) == o.jmask) a[j] = cmul(ph, a[j]);
-            }
-        }
+        run_program<R, RL, TL>(sm, sops, sset, nops, tid, a, P0, q);
         __syncthreads();
 #pragma unroll
-        for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = a[j];
+        for (int j = 0; j < NR; ++j) sm[reg_slot<RL>(P0, q, j)] = RegArith<R>::to_tile(a[j]);
         __syncthreads();
         C *gp = s + (insert_zeros((idx_t)tile, d.ins_pos, d.nins) | dt);
 #pragma unroll

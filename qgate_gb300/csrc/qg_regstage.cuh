@@ -73,6 +73,20 @@ __device__ __forceinline__ void reg_gate(C (&a)[NR], const MatR<R> &m, unsigned 
     }
 }
 
+// reg_gate with the matrix in the register arithmetic's own type.
+template <int I, int NR, class C>
+__device__ __forceinline__ void reg_gate_c(C (&a)[NR], const Mat2C<C> &m, unsigned jmask) {
+    if (jmask == 0) {
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+            if (!(j & (1 << I))) apply2c(m, a[j], a[j | (1 << I)]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+            if (!(j & (1 << I)) && (j & jmask) == jmask) apply2c(m, a[j], a[j | (1 << I)]);
+    }
+}
+
 template <int I, int NR, class C>
 __device__ __forceinline__ void reg_swap(C (&a)[NR], unsigned jmask) {
 #pragma unroll
