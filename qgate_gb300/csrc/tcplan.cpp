@@ -45,7 +45,8 @@ int stage_take(const std::vector<const PendingGate *> &gates, unsigned long long
     for (size_t i = 0; i < gates.size(); ++i) {
         const PendingGate *g = gates[i];
         if (i >= limit) {
-            if (keep) keep->push_back(g);
+            if (!keep) break;
+            keep->push_back(g);
             continue;
         }
         const unsigned long long q = gate_qmask(*g);
@@ -61,6 +62,22 @@ int stage_take(const std::vector<const PendingGate *> &gates, unsigned long long
 }
 
 
+// stage_take's count over precomputed lane masks: the same walk, stopped
+// once every lane of S is blocked (no later gate can be taken then).
+static int take_count(const std::vector<unsigned long long> &q, unsigned long long S) {
+    unsigned long long blocked = 0;
+    int count = 0;
+    for (const unsigned long long g : q) {
+        if ((g & blocked) || (g & ~S) || count >= kMaxStageGates) {
+            blocked |= g;
+            if ((blocked & S) == S) break;
+            continue;
+        }
+        ++count;
+    }
+    return count;
+}
+
 // Lane set (M lanes, including `base` and the first gate's lanes) of the next
 // tensor-core stage over `remaining` (see flush_lookahead).
 unsigned long long plan_stage_lanes(const std::vector<const PendingGate *> &remaining,
@@ -68,8 +85,14 @@ unsigned long long plan_stage_lanes(const std::vector<const PendingGate *> &rema
     const size_t kWindow = 512;
     const unsigned long long q0 = gate_qmask(*remaining[0]);
     unsigned long long cand_all = 0;
-    for (size_t i = 0; i < remaining.size() && i < kWindow; ++i)
-        cand_all |= gate_qmask(*remaining[i]);
+    std::vector<unsigned long long> qw;
+    qw.reserve(std::min(remaining.size(), kWindow));
+    for (size_t i = 0; i < remaining.size() && i < kWindow; ++i) {
+        qw.push_back(gate_qmask(*remaining[i]));
+        cand_all |= qw.back();
+    }
+    auto stage_take = [&](const std::vector<const PendingGate *> &, unsigned long long S, size_t,
+                          std::nullptr_t, std::nullptr_t) { return take_count(qw, S); };
     const unsigned long long fixed = base | q0;
     // Greedy growth from `S0`: add the lane that lets the stage take the
     // most gates until the stage has M lanes.
@@ -190,6 +213,13 @@ static unsigned short f16_bits(float x) {
     unsigned f;
     memcpy(&f, &x, 4);
     const unsigned sign = (f >> 16) & 0x8000u;
+    const unsigned a = f & 0x7fffffffu;
+    if (a - 0x38800000u < 0x477ff000u - 0x38800000u) {
+        // normal binary16 range (2^-14 <= |x| < 65520): round to nearest
+        // even at bit 13 with one add, then rebias the exponent (127 -> 15)
+        const unsigned r = a + 0xfffu + ((a >> 13) & 1u);
+        return (unsigned short)(sign | ((r - 0x38000000u) >> 13));
+    }
     const int e = (int)((f >> 23) & 0xffu) - 127 + 15;
     unsigned mant = f & 0x7fffffu;
     if (e >= 31) return (unsigned short)(sign | 0x7c00u);
@@ -209,9 +239,15 @@ static unsigned short f16_bits(float x) {
 }
 
 static double f16_value(unsigned short h) {
-    const int e = (h >> 10) & 31, mant = h & 1023;
-    double v = e == 0 ? std::ldexp((double)mant, -24) : std::ldexp((double)(mant | 1024), e - 25);
-    return (h & 0x8000u) ? -v : v;
+    const unsigned e = (h >> 10) & 31u, mant = h & 1023u;
+    float v;
+    if (e == 0) {
+        v = (float)mant * 5.9604644775390625e-8f;  // subnormal: mant * 2^-24, exact
+    } else {
+        const unsigned bits = ((e + 112u) << 23) | (mant << 13);  // rebias 15 -> 127
+        memcpy(&v, &bits, 4);
+    }
+    return (h & 0x8000u) ? -(double)v : (double)v;
 }
 
 // Split operand of a 32x32 complex block U (row-major, amplitude order of
