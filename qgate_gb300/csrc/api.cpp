@@ -1424,7 +1424,7 @@ int qg_circuit_new(int prec, int n_gates, const int *targets, const int *ctrl_of
 int qg_circuit_set_graph(qg_handle hc, int on) {
     QG_BEGIN
     Circuit *c = lookup(g_dev.circuits, hc, "circuit");
-    if (!on && c->graph) drop_graph(dev(), c);
+    if (!on && (c->exec || !c->chunks.empty())) drop_graph(dev(), c);
     c->graph = on != 0;
     QG_END
 }
@@ -1473,7 +1473,7 @@ int qg_circuit_stats(qg_handle hc, int *captured, int64_t *passes) {
 int qg_circuit_delete(qg_handle hc) {
     QG_BEGIN
     Circuit *c = lookup(g_dev.circuits, hc, "circuit");
-    drop_graph(dev(), c);
+    if (c->exec || !c->chunks.empty()) drop_graph(dev(), c);  // no device work otherwise
     g_dev.circuits.erase(c);
     delete c;
     QG_END

@@ -86,3 +86,31 @@ def test_known_answer_u_gate_equals_paulis_up_to_phase():
     assert np.allclose(nat.gate_matrix('U', (pi, pi / 2., pi / 2.)), -1j * nat.gate_matrix('Y'))
     assert np.allclose(nat.gate_matrix('U1', (pi,)), nat.gate_matrix('Z'))
     assert np.allclose(nat.gate_matrix('U2', (0., pi)), -1j * nat.gate_matrix('H'))
+
+
+def test_compiled_circuit_table_validation():
+    """qg_circuit_new checks the gate table as apply_controlled_gate checks a
+    call (lane range, control/target overlap, offsets) without touching the
+    device; a circuit that never ran is deleted without it too."""
+    from qgate_gb300 import _native as nat
+    from qgate_gb300.circuit import gate_type
+    from qgate_gb300.compiled import CompiledCircuit
+    h, x = gate_type('H'), gate_type('X')
+    c = CompiledCircuit(np.float64, [(h, False, 0, []), (x, False, 3, [0, 1]), (h, True, 61, [])],
+                        graph=False)
+    assert c.n_gates == 3
+    c.delete()
+    with pytest.raises(RuntimeError, match='overlapped'):
+        CompiledCircuit(np.float32, [(x, False, 2, [1, 2])], graph=False)
+    with pytest.raises(ValueError, match='out of range'):
+        CompiledCircuit(np.float32, [(h, False, 62, [])], graph=False)
+    with pytest.raises(ValueError, match='out of range'):
+        CompiledCircuit(np.float32, [(x, False, 1, [-1])], graph=False)
+    bad = nat.int_array([0, 1, 0])  # offsets must not decrease
+    t = nat.int_array([0, 1])
+    m = np.zeros(16)
+    with pytest.raises(ValueError, match='offsets'):
+        nat.new_handle('qg_circuit_new', nat.PREC_FP32, 2, nat.as_iptr(t), nat.as_iptr(bad),
+                       nat.as_iptr(nat.int_array([2])), nat.as_dptr(m))
+    with pytest.raises(ValueError, match='invalid circuit'):
+        nat.call('qg_circuit_run', 12345, 0)

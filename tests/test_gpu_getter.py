@@ -8,6 +8,7 @@ import pytest
 
 from oracle import statevec as sv
 from tests.gpu_helpers import ATOL, Lane, abs2, apply_ops, new_state, null, random_ops
+from tests.pool_model import fixed_point_samples
 
 pytestmark = pytest.mark.gpu
 
@@ -165,27 +166,6 @@ def test_sampling_pool_empty_lanes_and_random(rt, dtype):
     assert np.all((got & ((1 << 0) | (1 << 4) | (1 << 8))) == 0)
 
 
-def _fixed_point_samples(probs, u):
-    """The pool's sampling rule on exact integers: q = round(p * 2^60) (to
-    nearest, ties to even; exact in float64 for float32 and float64 p), P =
-    prefix sums of q, index = first i with P[i] > floor(u * P[-1]), clamped
-    to n - 1; negative and NaN u give 0."""
-    q = np.rint(probs.astype(np.float64) * 2.0 ** 60).astype(np.uint64)
-    P = np.cumsum(q, dtype=np.uint64)
-    T = int(P[-1])
-    out = np.zeros(len(u), np.int64)
-    for k, v in enumerate(np.asarray(u, np.float64)):
-        if not v >= 0.:
-            continue
-        if v >= 1.:
-            out[k] = len(P) - 1
-            continue
-        num, den = abs(float(v)).as_integer_ratio()
-        t = (num * T) // den
-        out[k] = min(int(np.searchsorted(P, np.uint64(t), side='right')), len(P) - 1)
-    return out
-
-
 EDGE_U = [0.0, -0.0, 1.0, 1.5, -0.5, float('nan'), 5e-324, 1. - 2. ** -53, 0.5]
 
 
@@ -208,7 +188,7 @@ def test_sampling_pool_fixed_point_exact(rt, dtype):
         pool = getter.create_sampling_pool(list(range(n)), n, 0, lanes, [])
         got = np.asarray(pool.sample(len(u), u).intarray)
         pool.delete()
-        assert np.array_equal(got, _fixed_point_samples(probs, u)), table[:2]
+        assert np.array_equal(got, fixed_point_samples(probs, u)), table[:2]
         prob_ref = sv.marginal_probabilities([(psi, table)], n, 0)
         want = sv.SamplingPool(prob_ref).sample(u[:100000])
         cdf_ref = np.cumsum(prob_ref) / prob_ref.sum()
@@ -236,7 +216,7 @@ def test_sampling_pool_fixed_point_exact_25q(rt):
     got = np.asarray(pool.sample(len(u), u).intarray)
     pool.delete()
     qs.delete()
-    assert np.array_equal(got, _fixed_point_samples(probs, u))
+    assert np.array_equal(got, fixed_point_samples(probs, u))
 
 
 @pytest.mark.parametrize('n, n_h, flips', [(14, 0, [3]), (20, 12, [15]), (25, 17, [20])],
@@ -261,7 +241,7 @@ def test_sampling_pool_guide_long_runs(rt, n, n_h, flips):
     got = np.asarray(pool.sample(len(u), u).intarray)
     pool.delete()
     qs.delete()
-    assert np.array_equal(got, _fixed_point_samples(probs, u))
+    assert np.array_equal(got, fixed_point_samples(probs, u))
     if n_h == 0:  # uniforms in [0, 1) select the basis state; >= 1: n - 1; < 0, NaN: 0
         ok = (u >= 0.) & (u < 1.)
         assert np.all(got[ok] == sum(1 << q for q in flips))
@@ -290,7 +270,7 @@ def test_sampling_pool_shifted_guide_entries(rt, k):
             got = np.asarray(pool.sample(len(u), u).intarray)
             pool.delete()
             qs.delete()
-            assert np.array_equal(got, _fixed_point_samples(probs, u))
+            assert np.array_equal(got, fixed_point_samples(probs, u))
     finally:
         nat.call('qg_set_pool_guide_index_shift', -1)
 
