@@ -199,9 +199,13 @@ template <> struct RegArith<double> {
     static __device__ __forceinline__ double2 to_tile(T v) {
         return make_double2(df_to(v.x), df_to(v.y));
     }
+    // the host packs (h, l) into an entry's 8 bytes little-endian: h low, l high
+    static __device__ __forceinline__ dfl unpack(double v) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+        return {__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32))};
+    }
     static __device__ __forceinline__ T entry(const double *m, int k) {
-        const float2 re = *(const float2 *)&m[2 * k], im = *(const float2 *)&m[2 * k + 1];
-        return {{re.x, re.y}, {im.x, im.y}};
+        return {unpack(m[2 * k]), unpack(m[2 * k + 1])};
     }
 };
 
