@@ -1,0 +1,221 @@
+// CPU checks of the tensor-stage host planner (qgate_gb300/csrc/tcplan.cpp),
+// built and run by tests/test_cpu_planner.py.  The planner file is included
+// whole so that its file-local helpers can be checked directly.  Prints
+// "<check> <value>" lines; FP16 rounding pairs go to the file named by argv[1]
+// for comparison with numpy.
+#include "tcplan.cpp"
+
+#include <cstdio>
+#include <random>
+#include <set>
+
+using namespace qg;
+typedef std::complex<double> cd;
+
+static PendingGate make_gate(int t, std::vector<int> c, cd a, cd b, cd cc, cd d) {
+    PendingGate g;
+    g.target = t;
+    g.controls = c;
+    const double v[8] = {a.real(), a.imag(), b.real(), b.imag(), cc.real(), cc.imag(), d.real(), d.imag()};
+    memcpy(g.m.v, v, sizeof(v));
+    g.diag = is_diag(g.m);
+    return g;
+}
+
+static std::vector<PendingGate> random_gates(std::mt19937 &rng, int n, int count) {
+    std::uniform_real_distribution<double> U(0, 6.283185307179586);
+    std::vector<PendingGate> out;
+    for (int i = 0; i < count; ++i) {
+        const int t = (int)(rng() % n);
+        std::vector<int> c;
+        const int nc = (int)(rng() % 3);
+        while ((int)c.size() < nc) {
+            int x = (int)(rng() % n);
+            if (x != t && std::find(c.begin(), c.end(), x) == c.end()) c.push_back(x);
+        }
+        const double th = U(rng), ph = U(rng), la = U(rng);
+        if (rng() % 4 == 0)  // diagonal
+            out.push_back(make_gate(t, c, 1., 0., 0., std::polar(1., ph)));
+        else
+            out.push_back(make_gate(t, c, std::cos(th / 2), -std::polar(std::sin(th / 2), la),
+                                    std::polar(std::sin(th / 2), ph),
+                                    std::polar(std::cos(th / 2), ph + la)));
+    }
+    return out;
+}
+
+int main(int argc, char **argv) {
+    std::mt19937 rng(2024);
+    // FP16 rounding: (float bits, f16 bits) pairs for numpy to check
+    {
+        FILE *f = fopen(argv[1], "wb");
+        std::uniform_real_distribution<double> u(-1, 1);
+        for (int i = 0; i < 200000; ++i) {
+            float x = (float)(u(rng) * std::ldexp(1.0, -(int)(rng() % 30)));
+            if (i % 5 == 0) {
+                unsigned b = (unsigned)rng();
+                memcpy(&x, &b, 4);
+                if (!std::isfinite(x) || std::fabs(x) > 6.0e4f) x = 0.f;
+            }
+            unsigned short h = f16_bits(x);
+            fwrite(&x, 4, 1, f);
+            fwrite(&h, 2, 1, f);
+        }
+        fclose(f);
+    }
+    // Split operands: Bh + Bl against the real form of a random unitary.
+    {
+        std::normal_distribution<double> g(0, 1);
+        static cd U[1024];
+        for (int i = 0; i < 32; ++i) {  // Gram-Schmidt rows of a random complex matrix
+            for (int k = 0; k < 32; ++k) U[i * 32 + k] = cd(g(rng), g(rng));
+            for (int j = 0; j < i; ++j) {
+                cd dot = 0;
+                for (int k = 0; k < 32; ++k) dot += std::conj(U[j * 32 + k]) * U[i * 32 + k];
+                for (int k = 0; k < 32; ++k) U[i * 32 + k] -= dot * U[j * 32 + k];
+            }
+            double nrm = 0;
+            for (int k = 0; k < 32; ++k) nrm += std::norm(U[i * 32 + k]);
+            for (int k = 0; k < 32; ++k) U[i * 32 + k] /= std::sqrt(nrm);
+        }
+        static unsigned short bh[4096], bl[4096];
+        tc_operand(U, bh, bl);
+        double worst = 0;
+        for (int o = 0; o < 32; ++o)
+            for (int i = 0; i < 32; ++i) {
+                const double val[2][2] = {{U[o * 32 + i].real(), -U[o * 32 + i].imag()},
+                                          {U[o * 32 + i].imag(), U[o * 32 + i].real()}};
+                for (int co = 0; co < 2; ++co)
+                    for (int ci = 0; ci < 2; ++ci) {
+                        const int n = 2 * o + co, k = 2 * i + ci;
+                        const size_t at = (size_t)(k / 16) * 1024 + (k % 16 / 8) * 512 +
+                                          (n / 8) * 64 + (n % 8) * 8 + k % 8;
+                        worst = std::max(worst, std::fabs(f16_value(bh[at]) + f16_value(bl[at]) -
+                                                          val[co][ci]));
+                    }
+            }
+        printf("operand_split_max_abs_err %.3e\n", worst);
+    }
+    // stage_take / plan_stage_lanes / tc_blocks on random gate lists.
+    int bad_partition = 0, bad_commute = 0, bad_count = 0, bad_lanes = 0, bad_blocks = 0;
+    for (int trial = 0; trial < 40; ++trial) {
+        const int n = 16 + (int)(rng() % 10), M = 12;
+        auto gates = random_gates(rng, n, 200 + (int)(rng() % 400));
+        std::vector<const PendingGate *> rem;
+        for (auto &g : gates) rem.push_back(&g);
+        const unsigned long long base = 15;
+        while (!rem.empty()) {
+            const unsigned long long q0 = gate_qmask(*rem[0]);
+            if (__builtin_popcountll(q0 | base) > M) {
+                rem.erase(rem.begin());
+                continue;
+            }
+            const unsigned long long S = plan_stage_lanes(rem, base, M);
+            if (__builtin_popcountll(S) > M || (S & (base | q0)) != (base | q0)) ++bad_lanes;
+            // the fast count equals stage_take's over the window, for S and neighbours
+            std::vector<unsigned long long> qw;
+            for (size_t i = 0; i < rem.size() && i < 512; ++i) qw.push_back(gate_qmask(*rem[i]));
+            for (int v = 0; v < 4; ++v) {
+                const unsigned long long T = v == 0 ? S : (S ^ (1ULL << (rng() % n)));
+                if (take_count(qw, T) != stage_take(rem, T, 512, nullptr, nullptr)) ++bad_count;
+            }
+            std::vector<const PendingGate *> take, keep;
+            stage_take(rem, S, rem.size(), &take, &keep);
+            // partition in order, taken gates inside S, nothing taken past a
+            // deferred gate that shares a lane with it
+            size_t it = 0, ik = 0;
+            unsigned long long blocked = 0;
+            for (auto *g : rem) {
+                const unsigned long long q = gate_qmask(*g);
+                if (it < take.size() && take[it] == g) {
+                    ++it;
+                    if (q & ~S) ++bad_lanes;
+                    if (q & blocked) ++bad_commute;
+                } else if (ik < keep.size() && keep[ik] == g) {
+                    ++ik;
+                    blocked |= q;
+                } else {
+                    ++bad_partition;
+                }
+            }
+            if (it != take.size() || ik != keep.size()) ++bad_partition;
+            if (take.size() > 1) {
+                unsigned long long SS = S;
+                for (int q = 0; q < n && __builtin_popcountll(SS) < M; ++q) SS |= 1ULL << q;
+                TileLanes tl = tile_lanes_of(SS, n);
+                auto blocks = tc_blocks(take, tl);
+                std::vector<const PendingGate *> seq;
+                for (auto &b : blocks) {
+                    if (__builtin_popcount(b.first) > 5) ++bad_blocks;
+                    for (auto *g : b.second) {
+                        unsigned q = 1u << tl.local_of[g->target];
+                        for (int c : g->controls) q |= 1u << tl.local_of[c];
+                        if (q & ~b.first) ++bad_blocks;
+                        seq.push_back(g);
+                    }
+                }
+                // the block order is a commutation-safe reordering of `take`
+                for (size_t a = 0; a < seq.size(); ++a)
+                    for (size_t b2 = a + 1; b2 < seq.size(); ++b2) {
+                        const auto pa = std::find(take.begin(), take.end(), seq[a]) - take.begin();
+                        const auto pb = std::find(take.begin(), take.end(), seq[b2]) - take.begin();
+                        if (pa > pb && (gate_qmask(*seq[a]) & gate_qmask(*seq[b2]))) ++bad_blocks;
+                    }
+            }
+            rem.swap(keep);
+        }
+    }
+    printf("bad_partition %d\nbad_commute %d\nbad_count %d\nbad_lanes %d\nbad_blocks %d\n",
+           bad_partition, bad_commute, bad_count, bad_lanes, bad_blocks);
+    // Operand slots of random layouts are bijections of the 4096 tile indices,
+    // and a launch plan's slot tables address every slot once per layout.
+    {
+        int bad_slots = 0;
+        for (int trial = 0; trial < 50; ++trial) {
+            std::vector<int> pos(12);
+            for (int i = 0; i < 12; ++i) pos[i] = i;
+            std::shuffle(pos.begin(), pos.end(), rng);
+            TcLayout L;
+            for (int i = 0; i < 8; ++i) L.rows[i] = i < 7 ? pos[i] : -1;
+            for (int k = 0; k < 5; ++k) L.amps[k] = pos[7 + k];
+            std::set<unsigned> seen;
+            for (unsigned ti = 0; ti < 4096; ++ti) seen.insert(tc_operand_slot(L, ti));
+            if (seen.size() != 4096 || *seen.rbegin() >= 4096) ++bad_slots;
+        }
+        int bad_tables = 0, launches = 0;
+        for (int trial = 0; trial < 10; ++trial) {
+            const int n = 20;
+            auto gates = random_gates(rng, n, 120);
+            std::vector<const PendingGate *> rem;
+            for (auto &g : gates) rem.push_back(&g);
+            const unsigned long long base = 15;
+            const unsigned long long S0 = plan_stage_lanes(rem, base, 12);
+            std::vector<const PendingGate *> take, keep;
+            stage_take(rem, S0, rem.size(), &take, &keep);
+            if (take.size() < 2) continue;
+            unsigned long long SS = S0;
+            for (int q = 0; q < n && __builtin_popcountll(SS) < 12; ++q) SS |= 1ULL << q;
+            TileLanes tl = tile_lanes_of(SS, n);
+            auto blocks = tc_blocks(take, tl);
+            const int nb = (int)std::min<size_t>(6, blocks.size());
+            static TcStageDesc desc;
+            static unsigned short ops[6 * 2 * 64 * 64];
+            tc_plan_launch(tl, n, blocks, 0, nb, desc, ops);
+            ++launches;
+            for (int b = 0; b <= nb + 1; ++b) {  // every set: 128 rows x 32 registers -> 4096 slots
+                const SetSlots &ss = desc.sets[b];
+                std::set<unsigned> seen;
+                for (unsigned r = 0; r < 128; ++r)
+                    for (unsigned j = 0; j < 32; ++j) {
+                        unsigned slot = (unsigned)ss.lo[r & 31u] ^ (unsigned)ss.hi[r >> 5];
+                        for (int k = 0; k < 5; ++k)
+                            if (j >> k & 1u) slot ^= ss.q[k];
+                        seen.insert(slot);
+                    }
+                if (seen.size() != 4096) ++bad_tables;
+            }
+        }
+        printf("bad_slots %d\nbad_tables %d\nlaunches_checked %d\n", bad_slots, bad_tables, launches);
+    }
+    return 0;
+}

@@ -1,0 +1,67 @@
+"""CPU checks of the tensor-stage host planner (tests/cpp/planner_check.cpp
+built against qgate_gb300/csrc/tcplan.cpp with the host compiler): FP16
+rounding of the block operands against numpy, the split operands' accuracy,
+the stage planner's partition and commutation safety, the fast gate count
+against stage_take, fused-block limits, and that every operand slot table is
+a bijection onto the 4096 slots of a tile (what the tensor-core kernel's
+shared-memory staging relies on)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, 'qgate_gb300', 'csrc')
+
+
+def _cuda_include():
+    for base in (os.environ.get('CUDA_HOME'), '/usr/local/cuda'):
+        if base and os.path.exists(os.path.join(base, 'include', 'cuda_runtime.h')):
+            return os.path.join(base, 'include')
+    return None
+
+
+@pytest.fixture(scope='module')
+def planner_run(tmp_path_factory):
+    cxx = shutil.which('g++')
+    inc = _cuda_include()
+    if not cxx or not inc:
+        pytest.skip('needs g++ and the CUDA headers')
+    d = tmp_path_factory.mktemp('planner')
+    exe = str(d / 'planner_check')
+    subprocess.run([cxx, '-O1', '-std=c++17', '-fopenmp', '-I', CSRC, '-I',
+                    os.path.join(ROOT, 'include'), '-I', inc,
+                    os.path.join(ROOT, 'tests', 'cpp', 'planner_check.cpp'), '-o', exe],
+                   check=True, capture_output=True)
+    pairs = str(d / 'f16.bin')
+    out = subprocess.run([exe, pairs], check=True, capture_output=True, text=True).stdout
+    vals = dict(line.split() for line in out.strip().splitlines())
+    return vals, pairs
+
+
+def test_fp16_rounding_matches_numpy(planner_run):
+    _, pairs = planner_run
+    rec = np.fromfile(pairs, dtype=np.dtype([('x', '<f4'), ('h', '<u2')]))
+    want = rec['x'].astype(np.float16).view(np.uint16)
+    assert np.array_equal(rec['h'], want)
+
+
+def test_split_operands_accuracy(planner_run):
+    vals, _ = planner_run
+    # FP16 hi + FP16 lo of entries <= 1: error below 2^-22 (relative) + lo's own rounding
+    assert float(vals['operand_split_max_abs_err']) < 2. ** -21
+
+
+def test_stage_planner_invariants(planner_run):
+    vals, _ = planner_run
+    for k in ('bad_partition', 'bad_commute', 'bad_count', 'bad_lanes', 'bad_blocks'):
+        assert int(vals[k]) == 0, k
+
+
+def test_operand_slot_tables_are_bijections(planner_run):
+    vals, _ = planner_run
+    assert int(vals['bad_slots']) == 0
+    assert int(vals['bad_tables']) == 0
+    assert int(vals['launches_checked']) >= 5
