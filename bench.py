@@ -533,10 +533,10 @@ def qft_ops(n, seed):
 def run_compiled(args, rt, nat):
     """Per-run latency of whole circuits through the plugin API with one call
     per gate (the reference front-end's pattern), against `CompiledCircuit`
-    (the gate table in one call) and its CUDA-graph replay: the 20-qubit QFT
-    of BASELINE config 0 (complex128 as specified, and complex64, where the
-    device work is small and the host's share shows; X preparation from
-    default_rng(0)) and the headline random circuit (complex64).  Wall time from reset to a
+    (the gate table in one call) and its CUDA-graph replay: the reference's
+    20-qubit QFT case (complex128, and complex64, where the device work is
+    small and the host's share shows; X preparation from default_rng(0)) and
+    the headline random circuit (complex64).  Wall time from reset to a
     synchronised state, median of the repeats after one warm-up run (which
     plans, and for the graph captures)."""
     from qgate_gb300.circuit import gate_type
