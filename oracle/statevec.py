@@ -1,6 +1,6 @@
 """CPU oracle: a numpy restatement of the reference's state-vector primitives.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker for the GB300 engine:
+TEST INFRASTRUCTURE ONLY.  This module is the oracle for the GB300 engine:
 only `tests/`, `__graft_entry__.smoke()` and the `cpu_baseline` leg of
 `bench.py` may import it.  The product (`qgate_gb300`) never calls it and has
 no CPU fallback.
