@@ -1,6 +1,6 @@
 """CPU oracle for expectations and gradients of parametrised circuits.
 
-TEST INFRASTRUCTURE ONLY (a checker; never called by the product).
+TEST INFRASTRUCTURE ONLY (part of the oracle; never called by the product).
 
 The reference has no gradient path: its users differentiate by running the
 circuit again with shifted parameters (parameter-shift) or by finite

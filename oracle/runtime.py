@@ -2,7 +2,7 @@
 runtime plugin protocol as the GB300 runtime and the reference's runtimes
 (qgate/simulator/pyruntime.py:10-328, qgate/simulator/native_*.py).
 
-TEST INFRASTRUCTURE ONLY — a checker, never part of the product.  Used by the
+TEST INFRASTRUCTURE ONLY — part of the oracle, never part of the product.  Used by the
 CPU tests to replay the reference's boundary traces (pinning the oracle to
 the reference's own outputs) and to produce expected values for GPU tests.
 """
