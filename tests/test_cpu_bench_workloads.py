@@ -1,0 +1,48 @@
+"""The bench's synthetic workloads match their specification (CPU only):
+the random U3 + CX circuit (angles from default_rng(10), CX matchings from
+default_rng(11), per layer), its unfused gate-pass byte count, and the QFT
+case (X preparation from default_rng(seed), then H and the controlled-U1
+ladder, no swaps), which the oracle turns into the uniform distribution."""
+import math
+
+import numpy as np
+
+import bench
+from oracle import statevec as sv
+
+
+def test_random_circuit_layers_follow_the_seeds():
+    n, depth = 30, 20
+    ops = bench.circuit(n, depth)
+    assert len(ops) == depth * (n + n // 2)
+    ang = np.random.default_rng(10).uniform(0, 2 * math.pi, (depth, n, 3))
+    prng = np.random.default_rng(11)
+    k = 0
+    for layer in range(depth):
+        for q in range(n):
+            name, args, target, ctrls = ops[k]
+            assert (name, target, ctrls) == ('U', q, ())
+            assert np.array_equal(np.asarray(args), ang[layer, q])
+            k += 1
+        p = prng.permutation(n)
+        for j in range(n // 2):
+            assert ops[k] == ('X', (), int(p[2 * j + 1]), (int(p[2 * j]),))
+            k += 1
+
+
+def test_gate_pass_bytes():
+    n = 30
+    ops = bench.circuit(n, 20)
+    want = 20 * (30 * 2 * (1 << n) * 8 + 15 * 2 * (1 << (n - 1)) * 8)
+    assert bench.gate_pass_bytes(n, ops, 8) == want
+
+
+def test_qft_case_gives_uniform_probabilities():
+    n = 10
+    ops = bench.qft_ops(n, 0)
+    rng = np.random.default_rng(0)
+    xs = [q for q in range(n) if rng.random() < 0.5]
+    assert [o[2] for o in ops[:len(xs)] if o[0] == 'X'] == xs
+    assert sum(1 for o in ops if o[0] == 'U1') == n * (n - 1) // 2
+    psi = sv.run_ops(n, [('g', nm, a, False, t, c) for nm, a, t, c in ops])
+    assert np.allclose(np.abs(psi) ** 2, 1. / (1 << n), atol=1e-12)
