@@ -23,17 +23,31 @@ from . import _native as nat
 from .gb300runtime import _matrix_entry, _prec
 
 
+def _matrix8(gate, adjoint):
+    """8 doubles (row-major, interleaved re/im) of a gate type or of a 2x2
+    complex matrix given directly."""
+    if isinstance(gate, np.ndarray):
+        m = np.asarray(gate, np.complex128)
+        if m.shape != (2, 2):
+            raise ValueError('a gate matrix must be 2x2, got {}.'.format(m.shape))
+        if adjoint:
+            m = m.conj().T
+        return np.stack([m.real, m.imag], axis=-1).reshape(-1)
+    return _matrix_entry(gate, adjoint)[0]
+
+
 class CompiledCircuit:
-    """gates: iterable of (gate_type, adjoint, target_lane, control_lanes),
-    the arguments of the runtime's apply_gate / apply_controlled_gate."""
+    """gates: iterable of (gate, adjoint, target_lane, control_lanes), the
+    arguments of the runtime's apply_gate / apply_controlled_gate; `gate` is
+    a qgate gate type or a 2x2 complex matrix (numpy array)."""
 
     def __init__(self, dtype, gates, graph=True):
         targets, offsets, ctrls, mats = [], [0], [], []
-        for gate_type, adjoint, target, controls in gates:
+        for gate, adjoint, target, controls in gates:
             targets.append(int(target))
             ctrls.extend(int(c) for c in controls)
             offsets.append(len(ctrls))
-            mats.append(_matrix_entry(gate_type, adjoint)[0])
+            mats.append(_matrix8(gate, adjoint))
         self.n_gates = len(targets)
         t = nat.int_array(targets)
         o = nat.int_array(offsets)

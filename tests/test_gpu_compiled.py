@@ -134,3 +134,33 @@ def test_compiled_circuit_errors(rt):
     assert psi[0] == 1. and np.count_nonzero(psi) == 1
     empty.delete()
     qs.delete()
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_qasm_programs_as_compiled_circuits(rt, dtype):
+    """OpenQASM 2.0 programs (qgate_gb300/qasm.py) lowered to compiled
+    circuits and run on the engine, against the oracle running the same
+    program ops: a 14-qubit QFT of a basis state and a mixed program with
+    user gates and multi-controlled standard gates."""
+    from qgate_gb300 import qasm
+    n = 14
+    lines = ['OPENQASM 2.0;', 'include "qelib1.inc";', 'qreg q[%d];' % n, 'x q[3]; x q[9];']
+    for i in range(n):
+        lines.append('h q[%d];' % i)
+        for j in range(i + 1, n):
+            lines.append('cu1(pi / %d) q[%d], q[%d];' % (1 << (j - i), j, i))
+    mixed = ('OPENQASM 2.0; include "qelib1.inc"; qreg a[7]; qreg b[7];\n'
+             'gate lay(t) x, y { ry(t) x; rz(-t / 3) y; cu3(t, t / 2, -t) x, y; }\n'
+             'h a; lay(0.7) a, b; ccx a[0], a[1], b[2]; cswap b[0], a[3], b[5];\n'
+             'crz(1.3) b[6], a[2]; rzz(0.4) a[4], b[4]; cy a[5], b[1]; sx b;\n')
+    for src in ('\n'.join(lines), mixed):
+        prog = qasm.parse(src)
+        want = sv.initial_state(prog.n_qubits, np.complex128)
+        for m, t, c in prog.ops:
+            sv.apply_controlled_gate(want, m, list(c), t)
+        with prog.compile(dtype, graph=True) as circ:
+            qs = new_state(rt, prog.n_qubits, dtype)
+            circ.run(qs)
+            got = _state(qs)
+            qs.delete()
+        assert np.allclose(got, want, atol=ATOL[dtype] * 8)
