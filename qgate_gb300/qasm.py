@@ -158,6 +158,7 @@ class _Parser:
         self.ops = []        # (matrix, target, controls)
         self.measured = {}   # qubit -> clbit
         self.touched = set()
+        self.depth = 0       # nesting of user-gate expansion
 
     # -- token helpers
     def peek(self, k=0):
@@ -428,9 +429,11 @@ class _Parser:
         elif name in self.gates:
             pnames, qnames, body = self.gates[name]
             arity(len(pnames), len(qnames))
+            if self.depth >= 64:
+                self.error('gate %r expands recursively' % name, tok)
             sub = _Parser.__new__(_Parser)
             sub.__dict__.update(self.__dict__)
-            sub.toks, sub.i = body, 0
+            sub.toks, sub.i, sub.depth = body, 0, self.depth + 1
             env = dict(zip(pnames, params))
             scope = dict(zip(qnames, lanes))
             while sub.peek()[0] != 'eof':

@@ -161,6 +161,7 @@ def test_rzz_and_user_gate_nesting():
     ('OPENQASM 2.0; qreg q[1]; gate g x { U(t, 0, 0) x; } g q[0];', 'unknown parameter'),
     ('OPENQASM 2.0; qreg q[2]; U(0, 0, 0) q[2];', 'out of range'),
     ('OPENQASM 2.0; qreg q[1]; qreg q[1];', 'declared twice'),
+    ('OPENQASM 2.0; qreg q[1]; gate g x { g x; } g q[0];', 'recursively'),
 ])
 def test_errors(src, msg):
     with pytest.raises(qasm.QasmError, match=msg):
