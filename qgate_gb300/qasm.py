@@ -157,6 +157,7 @@ class _Parser:
         self.std = False
         self.ops = []        # (matrix, target, controls)
         self.measured = {}   # qubit -> clbit
+        self.meas_order = []  # (qubit, clbit) in program order
         self.touched = set()
         self.depth = 0       # nesting of user-gate expansion
 
@@ -308,6 +309,7 @@ class _Parser:
                 self.error('measure of registers of different sizes', t)
             for q, c in zip(qs, cs):
                 self.measured[q] = c
+                self.meas_order.append((q, c))
         elif kw == 'reset':
             self.next()
             qs = self.argument(self.qregs, 'qreg')
@@ -451,14 +453,18 @@ class _Parser:
 class QasmProgram:
     """A parsed OpenQASM 2.0 program: `n_qubits` lanes, `ops` as (2x2
     complex128 matrix, target lane, control lanes) in program order,
-    `measurements` as (qubit, clbit) pairs, the register maps `qregs` /
+    `measurements` as (qubit, clbit) pairs by classical bit (a classical bit
+    written twice keeps the later measurement), the register maps `qregs` /
     `cregs` (name -> (first index, size))."""
 
     def __init__(self, p):
         self.n_qubits = p.n_qubits
         self.n_clbits = p.n_clbits
         self.ops = p.ops
-        self.measurements = sorted(p.measured.items())
+        last = {}
+        for q, c in p.meas_order:
+            last[c] = q
+        self.measurements = sorted(((q, c) for c, q in last.items()), key=lambda qc: qc[1])
         self.qregs = dict(p.qregs)
         self.cregs = dict(p.cregs)
 
@@ -466,6 +472,33 @@ class QasmProgram:
         """The ops in the form CompiledCircuit and apply_controlled_gate take:
         (matrix, adjoint flag, target lane, control lanes)."""
         return [(m, False, t, list(c)) for m, t, c in self.ops]
+
+    def sample(self, rt, qstates, shots, randnum=None):
+        """Draws `shots` outcomes of the program's measurements from
+        `qstates` (its state after the program ran), through the runtime's
+        sampling pool over the measured lanes (the other lanes summed out).
+        Returns int64 values with bit j = classical bit j; `randnum` are the
+        pool's uniforms (numpy's when None)."""
+        if not self.measurements:
+            raise QasmError('the program measures nothing.')
+        from .circuit import Lane
+        n = qstates.get_n_lanes()
+        qubits = sorted({q for q, _ in self.measurements})
+        if qubits[-1] >= n:
+            raise QasmError('the program measures qubit %d of a %d-lane state.' % (qubits[-1], n))
+        pos = {q: k for k, q in enumerate(qubits)}
+        lanes = [Lane(l, pos.get(l, -1)) for l in range(n)]
+        getter = rt.create_qubits_states_getter(qstates.processor.dtype)
+        pool = getter.create_sampling_pool(list(range(len(qubits))), len(qubits),
+                                           n - len(qubits), [(qstates, lanes)], [])
+        try:
+            idx = np.asarray(pool.sample(shots, randnum).intarray, np.int64)
+        finally:
+            pool.delete()
+        out = np.zeros(len(idx), np.int64)
+        for q, c in self.measurements:
+            out |= ((idx >> pos[q]) & 1) << c
+        return out
 
     def compile(self, dtype=np.float32, graph=True):
         """A CompiledCircuit of the program's gates (complex64 for float32)."""

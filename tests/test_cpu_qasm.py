@@ -181,3 +181,66 @@ def test_compiled_circuit_from_a_program():
     c = p.compile(np.float64, graph=False)
     assert c.n_gates == 5
     c.delete()
+
+
+class _FakeQstates:
+    """Stands in for a states object: the oracle's state vector."""
+
+    def __init__(self, psi):
+        self.psi = psi
+
+        class P:
+            dtype = np.float64
+        self.processor = P()
+
+    def get_n_lanes(self):
+        return int(self.psi.size).bit_length() - 1
+
+
+class _FakeRuntime:
+    """The runtime calls QasmProgram.sample makes, answered by the oracle:
+    the marginal over the pool lanes (hidden lanes summed out) and its FP64
+    sampling pool."""
+
+    def create_qubits_states_getter(self, dtype):
+        return self
+
+    def create_sampling_pool(self, ordering, n_lanes, n_hidden, lane_trans, empty):
+        (qs, lanes), = lane_trans
+        assert empty == [] and n_lanes + n_hidden == qs.get_n_lanes()
+        h = n_lanes
+        table = []
+        for ln in lanes:
+            if ln.external == -1:
+                table.append(h)
+                h += 1
+            else:
+                table.append(ln.external)
+        prob = sv.marginal_probabilities([(qs.psi, table)], n_lanes, n_hidden)
+        pool = sv.SamplingPool(prob)
+
+        class Pool:
+            def sample(self, shots, u):
+                class Obs:
+                    intarray = pool.sample(u[:shots])
+                return Obs()
+
+            def delete(self):
+                pass
+        return Pool()
+
+
+def test_sample_maps_measured_lanes_to_classical_bits():
+    src = ('OPENQASM 2.0; include "qelib1.inc"; qreg q[4]; creg c[3]; h q[2]; '
+           'cx q[2], q[0]; x q[3]; measure q[0] -> c[2]; measure q[2] -> c[0]; '
+           'measure q[3] -> c[1]; measure q[1] -> c[1];')
+    prog = qasm.parse(src)
+    assert prog.measurements == [(2, 0), (1, 1), (0, 2)]  # c[1] keeps the later q[1]
+    qs = _FakeQstates(run(prog))
+    u = np.random.default_rng(4).random(4000)
+    out = prog.sample(_FakeRuntime(), qs, len(u), u)
+    # q[0] = q[2] (GHZ pair) -> c[2] = c[0]; q[1] = 0 -> c[1] = 0
+    assert set(np.unique(out)) == {0b000, 0b101}
+    assert 0.45 < np.mean(out == 0b101) < 0.55
+    with pytest.raises(qasm.QasmError, match='measures nothing'):
+        qasm.parse('OPENQASM 2.0; qreg q[1];').sample(_FakeRuntime(), qs, 1)
