@@ -31,9 +31,9 @@ CANDIDATES = {
                  (12, 5, 0, 0, 0), (13, 4, 0, 0, 0), (13, 5, 0, 0, 0), (12, 4, 130, 0, 0),
                  (11, 4, 130, 0, 0), (12, 5, 0, 1, 0), (12, 5, 0, 1, 1), (13, 5, 0, 1, 0)],
     np.float64: [(10, 4, 0, 0, 0), (11, 4, 0, 0, 0), (12, 4, 0, 0, 0), (13, 4, 0, 0, 0),
-                 (11, 3, 0, 0, 0)],
+                 (11, 3, 0, 0, 0), (12, 3, 0, 0, 0)],
 }
-_VERSION = 'v2'
+_VERSION = 'v3'
 
 
 def _norm(c):
