@@ -8,6 +8,10 @@ runtime plugin protocol.
   loaded by `qgate_gb300._native`; importing that module (or anything that
   uses the engine) fails loudly if the library has not been built.
 * `qgate_gb300.csrc.build` builds the library in-tree.
+* Beyond the runtime protocol: `compiled` (a gate table applied in one call,
+  CUDA-graph replay), `qasm` (OpenQASM 2.0 programs lowered to compiled
+  circuits), `adjoint` (batched adjoint gradients), `batch` (many small
+  circuits in one launch sequence), `autotune` (fused-stage shapes).
 """
 
 __all__ = ['simulator']
