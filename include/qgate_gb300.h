@@ -295,11 +295,16 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
  * partials go to a fixed 2048-double (16 KiB) device array that each GPU
  * holds from library load until process exit.  The reduction uses at most
  * 1216 of those partials for any state size; n_lanes must be in [1, 40] and
- * anything else is rejected with QG_ERR_VALUE.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that
- * device current, so make that first call before any stream capture.  All
- * calls share the one array: calls whose work overlaps on the GPU (different
- * streams, no ordering between them) race on it and give wrong results. */
+ * anything else is rejected with QG_ERR_VALUE, as are a d_state that is not
+ * 16-byte aligned and a d_prob that is not 8-byte aligned (the kernel reads
+ * the state as 16-byte vectors).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current and
+ * keeps it for the life of the process, so make that first call before any
+ * stream capture; a cudaDeviceReset() on that device invalidates the kept
+ * address, and the entry point must not be called on that device after one.
+ * All calls share the one array: calls whose work overlaps on the GPU
+ * (different streams, no ordering between them) race on it and give wrong
+ * results. */
 int qg_calc_probability_noalloc(int prec, const void *d_state, int n_lanes, int local_lane,
                                 double *d_prob, uint64_t stream);
 

@@ -75,6 +75,17 @@ extern "C" int qg_calc_probability_noalloc(int prec, const void *d_state, int n_
         set_last_error("null state or output pointer");
         return QG_ERR_VALUE;
     }
+    // The reduction reads the state as 16-byte vectors (two complex64 or one
+    // complex128 amplitude) and writes one double: a misaligned pointer would
+    // fault inside the kernel, so it is refused here, before any launch.
+    if (((uintptr_t)d_state & 15u) != 0u) {
+        set_last_error("d_state must be 16-byte aligned");
+        return QG_ERR_VALUE;
+    }
+    if (((uintptr_t)d_prob & 7u) != 0u) {
+        set_last_error("d_prob must be 8-byte aligned");
+        return QG_ERR_VALUE;
+    }
     if (n_lanes < 1 || n_lanes > 40) {
         set_last_error("n_lanes must be in [1, 40]");
         return QG_ERR_VALUE;

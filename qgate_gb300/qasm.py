@@ -74,6 +74,11 @@ def _u1(lam):
     return np.array([[1, 0], [0, np.exp(1j * lam)]], np.complex128)
 
 
+# Upper bound on the gates one program may expand to: user gates that call
+# each other several times grow exponentially with nesting depth, and this
+# stops such a program with a parse error instead of exhausting host memory.
+MAX_OPS = 50_000_000
+
 _X = np.array([[0, 1], [1, 0]], np.complex128)
 _Y = np.array([[0, -1j], [1j, 0]], np.complex128)
 _Z = np.array([[1, 0], [0, -1]], np.complex128)
@@ -415,6 +420,8 @@ class _Parser:
                 if q in self.measured:
                     self.error('gate on qubit %d after its measurement' % q, tok)
                 self.touched.add(q)
+            if len(self.ops) >= MAX_OPS:
+                self.error('program expands to more than %d gates' % MAX_OPS, tok)
             self.ops.append((mat, target, tuple(controls)))
 
         def arity(np_, nq):

@@ -168,6 +168,17 @@ def test_errors(src, msg):
         qasm.parse(src)
 
 
+def test_exponential_expansion_is_stopped(monkeypatch):
+    """User gates that each call the previous one twice double the gate count
+    per level: the parser stops at its gate cap with a parse error."""
+    monkeypatch.setattr(qasm, 'MAX_OPS', 1000)
+    src = 'OPENQASM 2.0; qreg q[1]; gate g0 x { U(0.1, 0, 0) x; } '
+    for k in range(1, 16):
+        src += 'gate g%d x { g%d x; g%d x; } ' % (k, k - 1, k - 1)
+    with pytest.raises(qasm.QasmError, match='more than 1000 gates'):
+        qasm.parse(src + 'g15 q[0];')
+
+
 def test_reset_of_a_fresh_qubit_and_terminal_measurements():
     p = qasm.parse('OPENQASM 2.0; include "qelib1.inc"; qreg q[2]; creg c[2]; reset q; '
                    'h q[0]; cx q[0], q[1]; barrier q; measure q -> c;')

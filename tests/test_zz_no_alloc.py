@@ -51,3 +51,19 @@ def test_noalloc_rejects_out_of_range_sizes(rt):
         nat.call('qg_calc_probability_noalloc', nat.PREC_FP32, 16, 41, 0, 16, 0)
     with pytest.raises(ValueError, match='local_lane'):
         nat.call('qg_calc_probability_noalloc', nat.PREC_FP32, 16, 4, 4, 16, 0)
+
+
+def test_noalloc_rejects_misaligned_pointers(rt):
+    """A complex64 state that starts 8 bytes into a buffer (a slice from the
+    second amplitude) is refused on the host before any launch, as is an
+    output pointer that is not 8-byte aligned; nothing runs on the GPU."""
+    import torch
+    from qgate_gb300 import _native as nat
+    state = torch.zeros(1 << 6, dtype=torch.complex64, device='cuda')
+    out = torch.zeros(2, dtype=torch.float64, device='cuda')
+    with pytest.raises(ValueError, match='16-byte aligned'):
+        nat.call('qg_calc_probability_noalloc', nat.PREC_FP32, state.data_ptr() + 8, 5, 0,
+                 out.data_ptr(), 0)
+    with pytest.raises(ValueError, match='8-byte aligned'):
+        nat.call('qg_calc_probability_noalloc', nat.PREC_FP32, state.data_ptr(), 5, 0,
+                 out.data_ptr() + 4, 0)
