@@ -39,6 +39,8 @@ def lib():
         L.cs_prefix_sum_normalise.argtypes = [vp, i64]
         L.cs_prefix_sum_normalise.restype = d
         L.cs_sample.argtypes = [vp, i64, vp, vp, i64, vp, i]
+        L.cs_run_circuit.argtypes = [vp, i, i, i, vp, vp, vp, vp, i]
+        L.cs_run_circuit.restype = i
         _lib = L
     return _lib
 
@@ -62,6 +64,23 @@ class State:
         lib().cs_apply_gate(self.psi.ctypes.data, self.n, self.prec, m.ctypes.data,
                             c.ctypes.data if c.size else None, int(c.size), int(target))
 
+    def run(self, gates, max_lanes=14):
+        """Applies [(2x2 matrix, target, controls)] in order, in cache-sized
+        passes (cs_run_circuit: the same result as one apply() per gate).
+        Returns the number of passes."""
+        mats = np.ascontiguousarray(np.array([np.asarray(m, np.complex128).reshape(4)
+                                              for m, _, _ in gates]).reshape(-1)).view(np.float64)
+        targets = np.ascontiguousarray([t for _, t, _ in gates], np.int32)
+        off = np.zeros(len(gates) + 1, np.int32)
+        off[1:] = np.cumsum([len(c) for _, _, c in gates])
+        ctrls = np.ascontiguousarray([q for _, _, c in gates for q in c] or [0], np.int32)
+        r = lib().cs_run_circuit(self.psi.ctypes.data, self.n, self.prec, len(gates),
+                                 mats.ctypes.data, targets.ctypes.data, off.ctypes.data,
+                                 ctrls.ctypes.data, max_lanes)
+        if r < 0:
+            raise ValueError('max_lanes must be in [5, 20]')
+        return r
+
     def calc_probability(self, lane):
         return lib().cs_calc_probability(self.psi.ctypes.data, self.n, self.prec, lane)
 
@@ -69,6 +88,26 @@ class State:
         out = np.empty(1 << self.n, np.float64)
         lib().cs_probabilities(self.psi.ctypes.data, self.n, self.prec, out.ctypes.data)
         return out
+
+
+def prefix_cdf(prob, copy=True):
+    """(cdf, total): the reference pool's normalised FP64 prefix sums of
+    `prob` (cs_prefix_sum_normalise); copy=False overwrites a contiguous
+    float64 `prob` in place."""
+    cdf = np.array(prob, np.float64) if copy else np.ascontiguousarray(prob, np.float64)
+    total = lib().cs_prefix_sum_normalise(cdf.ctypes.data, cdf.size)
+    return cdf, total
+
+
+def sample_cdf(cdf, u, empty_lanes=()):
+    """Indices the reference pool draws for uniforms `u` from a normalised
+    CDF (cs_sample: upper_bound, clamped, empty-lane bits inserted)."""
+    u = np.ascontiguousarray(u, np.float64)
+    obs = np.empty(u.size, np.int64)
+    e = np.ascontiguousarray(np.asarray(empty_lanes, np.int32))
+    lib().cs_sample(cdf.ctypes.data, cdf.size, u.ctypes.data, obs.ctypes.data, u.size,
+                    e.ctypes.data if e.size else None, int(e.size))
+    return obs
 
 
 def sampling_pool_sample(prob, u, empty_lanes=()):

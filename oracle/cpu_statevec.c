@@ -110,6 +110,140 @@ void cs_apply_gate(void *state, int n, int prec, const double *m, const int *ctr
     }
 }
 
+/* A whole circuit, in passes over blocks of the state that stay in the
+ * core's cache: consecutive gates whose lanes, together with lanes 0..3, fit
+ * in `max_lanes` lanes form a pass; the pass's lane set is padded with the
+ * lowest free lanes, and for every assignment of the other lanes the pass
+ * applies its gates in order to that 2^max_lanes-amplitude block.  Each
+ * amplitude pair sees exactly the updates of cs_apply_gate (the same
+ * expressions, qgate/simulator/src/CPUQubitProcessor.cpp:307-362) in the
+ * same gate order, so the result equals one cs_apply_gate sweep per gate; it
+ * only moves the state through memory once per pass instead of once per
+ * gate.  Gate g: matrix mats[8g..8g+8) (as cs_apply_gate), target
+ * targets[g], controls ctrls[ctrl_off[g]..ctrl_off[g+1]). */
+#define PAIR_UPDATE(R, i0, i1)                                                           \
+    {                                                                                    \
+        R ar = s[2 * (i0)], ai = s[2 * (i0) + 1], br = s[2 * (i1)], bi = s[2 * (i1) + 1];     \
+        s[2 * (i0)] = m00r * ar - m00i * ai + m01r * br - m01i * bi;                     \
+        s[2 * (i0) + 1] = m00r * ai + m00i * ar + m01r * bi + m01i * br;                 \
+        s[2 * (i1)] = m10r * ar - m10i * ai + m11r * br - m11i * bi;                     \
+        s[2 * (i1) + 1] = m10r * ai + m10i * ar + m11r * bi + m11i * br;                 \
+    }
+/* Local index i = h * 2^L + l: l runs over the block's L contiguous low
+ * lanes (consecutive amplitudes), h over its other lanes (dep[h << L]). */
+#define PASS_BODY(R)                                                                     \
+    R *s = (R *)state;                                                                   \
+    _Pragma("omp parallel for schedule(static)")                                         \
+    for (idx_t o = 0; o < n_outer; ++o) {                                                \
+        const idx_t base = insert_zeros(o, pos, K);                                      \
+        for (int g = g0; g < g1; ++g) {                                                  \
+            const double *m = mats + 8 * (size_t)g;                                      \
+            SETUP(R)                                                                     \
+            const idx_t tl = ltb[g - g0], cm = lcm[g - g0];                              \
+            const idx_t cmh = cm >> L, cml = cm & (nlow - 1);                            \
+            if (tl >= nlow) {                                                            \
+                const idx_t th = tl >> L;                                                \
+                for (idx_t h = 0; h < nhigh; ++h) {                                      \
+                    if ((h & th) || (h & cmh) != cmh) continue;                          \
+                    const idx_t p0 = base + dep[h << L], p1 = base + dep[(h | th) << L];  \
+                    if (cml) {                                                           \
+                        for (idx_t l = 0; l < nlow; ++l)                                 \
+                            if ((l & cml) == cml) PAIR_UPDATE(R, p0 + l, p1 + l)         \
+                    } else {                                                             \
+                        for (idx_t l = 0; l < nlow; ++l) PAIR_UPDATE(R, p0 + l, p1 + l)  \
+                    }                                                                    \
+                }                                                                        \
+            } else {                                                                     \
+                for (idx_t h = 0; h < nhigh; ++h) {                                      \
+                    if ((h & cmh) != cmh) continue;                                      \
+                    const idx_t p = base + dep[h << L];                                  \
+                    if (cml) {                                                           \
+                        for (idx_t l0 = 0; l0 < nlow; l0 += 2 * tl)                       \
+                            for (idx_t l = l0; l < l0 + tl; ++l)                         \
+                                if ((l & cml) == cml) PAIR_UPDATE(R, p + l, p + l + tl)  \
+                    } else if (tl == 1) {                                                \
+                        for (idx_t l = 0; l < nlow; l += 2) PAIR_UPDATE(R, p + l, p + l + 1) \
+                    } else {                                                             \
+                        for (idx_t l0 = 0; l0 < nlow; l0 += 2 * tl)                       \
+                            for (idx_t l = l0; l < l0 + tl; ++l)                         \
+                                PAIR_UPDATE(R, p + l, p + l + tl)                        \
+                    }                                                                    \
+                }                                                                        \
+            }                                                                            \
+        }                                                                                \
+    }
+
+static idx_t gate_lanes(const int *targets, const int *ctrl_off, const int *ctrls, int g) {
+    idx_t q = (idx_t)1 << targets[g];
+    for (int c = ctrl_off[g]; c < ctrl_off[g + 1]; ++c) q |= (idx_t)1 << ctrls[c];
+    return q;
+}
+
+int cs_run_circuit(void *state, int n, int prec, int n_gates, const double *mats,
+                   const int *targets, const int *ctrl_off, const int *ctrls, int max_lanes) {
+    if (max_lanes > n) max_lanes = n;
+    if (max_lanes < 5 || max_lanes > 20) return -1;
+    const idx_t low = ((idx_t)1 << (n < 4 ? n : 4)) - 1;
+    int passes = 0;
+    idx_t *dep = (idx_t *)malloc(sizeof(idx_t) << max_lanes);
+    idx_t *ltb = (idx_t *)malloc(sizeof(idx_t) * (size_t)(n_gates > 0 ? n_gates : 1));
+    idx_t *lcm = (idx_t *)malloc(sizeof(idx_t) * (size_t)(n_gates > 0 ? n_gates : 1));
+    for (int g0 = 0; g0 < n_gates;) {
+        idx_t S = low;
+        int g1 = g0;
+        while (g1 < n_gates) {
+            const idx_t q = gate_lanes(targets, ctrl_off, ctrls, g1);
+            if (__builtin_popcountll(S | q) > max_lanes) break;
+            S |= q;
+            ++g1;
+        }
+        if (g1 == g0) { /* a gate wider than the pass: its lanes alone */
+            S = gate_lanes(targets, ctrl_off, ctrls, g0);
+            g1 = g0 + 1;
+        }
+        for (int q = 0; q < n && __builtin_popcountll(S) < max_lanes; ++q) S |= (idx_t)1 << q;
+        int pos[64], K = 0, local_of[64];
+        for (int q = 0; q < n; ++q) {
+            local_of[q] = -1;
+            if (S >> q & 1) {
+                local_of[q] = K;
+                pos[K++] = q;
+            }
+        }
+        const idx_t nloc = (idx_t)1 << K, n_outer = (idx_t)1 << (n - K);
+        int L = 0;
+        while (L < K && pos[L] == L) ++L;
+        const idx_t nlow = (idx_t)1 << L, nhigh = (idx_t)1 << (K - L);
+        for (idx_t i = 0; i < nloc; ++i) {
+            idx_t off = 0;
+            for (int k = 0; k < K; ++k)
+                if (i >> k & 1) off |= (idx_t)1 << pos[k];
+            dep[i] = off;
+        }
+        for (int g = g0; g < g1; ++g) {
+            ltb[g - g0] = (idx_t)1 << local_of[targets[g]];
+            idx_t cm = 0;
+            for (int c = ctrl_off[g]; c < ctrl_off[g + 1]; ++c) cm |= (idx_t)1 << local_of[ctrls[c]];
+            lcm[g - g0] = cm;
+        }
+#define SETUP(R)                                                                \
+    const R m00r = (R)m[0], m00i = (R)m[1], m01r = (R)m[2], m01i = (R)m[3];     \
+    const R m10r = (R)m[4], m10i = (R)m[5], m11r = (R)m[6], m11i = (R)m[7];
+        if (prec == 1) {
+            PASS_BODY(double)
+        } else {
+            PASS_BODY(float)
+        }
+#undef SETUP
+        ++passes;
+        g0 = g1;
+    }
+    free(dep);
+    free(ltb);
+    free(lcm);
+    return passes;
+}
+
 /* Pr(lane == 0): qgate/simulator/src/CPUQubitProcessor.cpp:75-125 (the
  * reference accumulates per thread in the state's precision; FP64 here). */
 double cs_calc_probability(const void *state, int n, int prec, int lane) {
