@@ -13,10 +13,22 @@ become available; they are implemented here from their definitions as
 matrices), `qreg` / `creg`, the built-ins `U(theta, phi, lambda)` and `CX`,
 user `gate` definitions with parameters (expanded as macros), register
 broadcasting, expressions (+ - * / ^, unary -, pi, sin cos tan exp ln sqrt),
-`barrier` (ignored), `measure` at the end of a qubit's gates (recorded as
-(qubit, clbit) pairs), `reset` of a qubit that no gate has touched yet (a
-no-op).  Not supported in a compiled circuit: `if`, `opaque`, mid-circuit
-measurement or reset -- they raise QasmError.
+`barrier` (ignored), `measure`, `reset` and `if (creg == n) qop` anywhere,
+as the reference's grammar accepts them (qgate/openqasm/yacc.py:74, :82-91,
+:115-124).  `opaque` raises QasmError.
+
+A program whose measurements all come after the gates of their qubits (and
+that has no `if` and no reset of a used qubit) is static: its gates form one
+compiled circuit (`compile()`) and its measurements are drawn from the final
+state by a sampling pool (`sample()`).  Any program runs shot by shot with
+`run()`, which executes the gates in compiled segments and the measurements,
+resets and conditions in between with the runtime's own operations, under
+the reference's rules (qgate/simulator/rop_executor.py:36-53,
+qgate/simulator/model_executor.py:117-136): a measurement draws u and
+returns 0 iff u < Pr(qubit = 0), then collapses the state (decohere); a reset
+needs the qubit measured and moves a |1> outcome back to |0> (apply_reset);
+`if (c == n)` runs its operation when the register c, read as an integer with
+c[0] the least significant bit, equals n.
 
 Conventions (OpenQASM 2.0): U(t, p, l) = [[cos(t/2), -e^{il} sin(t/2)],
 [e^{ip} sin(t/2), e^{i(p+l)} cos(t/2)]]; u1(l) = diag(1, e^{il});
@@ -161,9 +173,13 @@ class _Parser:
         self.gates = {}      # user gates: name -> (params, qargs, body tokens)
         self.std = False
         self.ops = []        # (matrix, target, controls)
+        self.items = []      # the program: ('g', matrix, target, controls),
+        #                      ('m', qubit, clbit), ('r', qubit),
+        #                      ('if', first clbit, size, value, [items])
         self.measured = {}   # qubit -> clbit
         self.meas_order = []  # (qubit, clbit) in program order
         self.touched = set()
+        self.flags = {'dynamic': False}
         self.depth = 0       # nesting of user-gate expansion
 
     # -- token helpers
@@ -299,12 +315,35 @@ class _Parser:
         elif kw == 'opaque':
             self.error('opaque gates cannot be simulated', t)
         elif kw == 'if':
-            self.error('classically controlled gates are not supported in a compiled circuit', t)
+            self.next()
+            self.expect('(')
+            c = self.expect(kind='id')
+            if c[1] not in self.cregs:
+                self.error('unknown creg %r' % c[1], c)
+            self.expect('==')
+            value = int(self.expect(kind='int')[1])
+            self.expect(')')
+            first, size = self.cregs[c[1]]
+            body = []
+            outer, self.items = self.items, body
+            try:
+                self.qop()
+            finally:
+                self.items = outer
+            self.flags['dynamic'] = True
+            self.items.append(('if', first, size, value, body))
         elif kw == 'barrier':
             self.next()
             self.args_any()
             self.expect(';')
-        elif kw == 'measure':
+        else:
+            self.qop()
+
+    def qop(self):
+        """One quantum operation: a gate application, `measure` or `reset`."""
+        t = self.peek()
+        kw = t[1] if t[0] == 'id' else None
+        if kw == 'measure':
             self.next()
             qs = self.argument(self.qregs, 'qreg')
             self.expect('->')
@@ -315,13 +354,17 @@ class _Parser:
             for q, c in zip(qs, cs):
                 self.measured[q] = c
                 self.meas_order.append((q, c))
+                self.items.append(('m', q, c))
         elif kw == 'reset':
             self.next()
             qs = self.argument(self.qregs, 'qreg')
             self.expect(';')
             for q in qs:
                 if q in self.touched or q in self.measured:
-                    self.error('reset after gates is not supported in a compiled circuit', t)
+                    self.flags['dynamic'] = True
+                self.items.append(('r', q))
+        elif kw in ('if', 'barrier', 'qreg', 'creg', 'gate', 'opaque', 'include'):
+            self.error('%r cannot follow if (...)' % kw, t)
         else:
             self.gate_call({}, None)
 
@@ -418,11 +461,12 @@ class _Parser:
         def emit(mat, target, controls):
             for q in (target,) + tuple(controls):
                 if q in self.measured:
-                    self.error('gate on qubit %d after its measurement' % q, tok)
+                    self.flags['dynamic'] = True  # a gate after a measurement
                 self.touched.add(q)
             if len(self.ops) >= MAX_OPS:
                 self.error('program expands to more than %d gates' % MAX_OPS, tok)
             self.ops.append((mat, target, tuple(controls)))
+            self.items.append(('g', mat, target, tuple(controls)))
 
         def arity(np_, nq):
             if len(params) != np_ or len(lanes) != nq:
@@ -462,18 +506,177 @@ class QasmProgram:
     complex128 matrix, target lane, control lanes) in program order,
     `measurements` as (qubit, clbit) pairs by classical bit (a classical bit
     written twice keeps the later measurement), the register maps `qregs` /
-    `cregs` (name -> (first index, size))."""
+    `cregs` (name -> (first index, size)), `items` (the whole program in
+    order: ('g', matrix, target, controls), ('m', qubit, clbit),
+    ('r', qubit), ('if', first clbit, size, value, [items])) and `dynamic`
+    (True when measurements, resets or conditions sit between gates, so the
+    program must run shot by shot with `run()`)."""
 
     def __init__(self, p):
         self.n_qubits = p.n_qubits
         self.n_clbits = p.n_clbits
         self.ops = p.ops
+        self.items = p.items
+        self.dynamic = p.flags['dynamic']
         last = {}
         for q, c in p.meas_order:
             last[c] = q
         self.measurements = sorted(((q, c) for c, q in last.items()), key=lambda qc: qc[1])
         self.qregs = dict(p.qregs)
         self.cregs = dict(p.cregs)
+        self._segments = {}
+
+    def _static_only(self, what):
+        if self.dynamic:
+            raise QasmError('%s needs a program without mid-circuit measurements, resets of '
+                            'used qubits or if; run it shot by shot with run().' % what)
+
+    def _plan(self, items, dtype, graph):
+        """items with each run of consecutive gates replaced by one
+        ('c', CompiledCircuit) segment (built once per precision)."""
+        from .compiled import CompiledCircuit
+        out, run = [], []
+
+        def close():
+            if run:
+                out.append(('c', CompiledCircuit(dtype, [(m, False, t, list(c))
+                                                         for m, t, c in run], graph=graph),
+                            list(run)))
+                run.clear()
+        for it in items:
+            if it[0] == 'g':
+                run.append(it[1:])
+                continue
+            close()
+            if it[0] == 'if':
+                out.append(('if',) + it[1:4] + (self._plan(it[4], dtype, graph),))
+            else:
+                out.append(it)
+        close()
+        return out
+
+    def run(self, qstates, randnum=None, graph=False, gate_runner=None):
+        """Runs the program once on `qstates` (at least n_qubits lanes, in
+        the state the program starts from -- normally |0...0>) and returns
+        the classical register as an int (bit j = classical bit j).
+
+        Gates run as compiled segments (CUDA-graph replay with graph=True);
+        `gate_runner(qstates, [(matrix, target, controls)])`, when given,
+        applies each segment instead.  A measurement takes the next uniform
+        from `randnum` (an iterable of floats in [0, 1); numpy's global RNG
+        when None, as the reference front-end draws them) and follows the
+        reference: outcome 0 iff u < Pr(qubit = 0), then decohere; the
+        qubit's lane state records the outcome.  A reset of a qubit measured
+        1 applies the runtime's reset, of a qubit measured 0 or still in
+        |0> (never touched, or reset since) does nothing; a reset of any
+        other qubit raises RuntimeError('Qubit is not measured.'), as the
+        reference does.  A gate on a measured qubit clears its lane state."""
+        proc = qstates.processor
+        if qstates.get_n_lanes() < self.n_qubits:
+            raise QasmError('the program has %d qubits, the state %d lanes.'
+                            % (self.n_qubits, qstates.get_n_lanes()))
+        if gate_runner is None:
+            key = (proc.dtype, bool(graph))
+            if key not in self._segments:
+                self._segments[key] = self._plan(self.items, proc.dtype, graph)
+            prog = self._segments[key]
+        else:
+            prog = self._plan_host(self.items)
+        uniforms = iter(randnum) if randnum is not None else None
+        clbits = [0] * self.n_clbits
+        lane_state = {}
+        known_zero = set(range(self.n_qubits))
+
+        def execute(items):
+            for it in items:
+                kind = it[0]
+                if kind in ('c', 'h'):
+                    for _, t, c in it[2]:
+                        for q in (t,) + tuple(c):
+                            lane_state.pop(q, None)
+                            known_zero.discard(q)
+                    if kind == 'c':
+                        it[1].run(qstates)
+                    else:
+                        gate_runner(qstates, it[2])
+                elif kind == 'm':
+                    q, c = it[1], it[2]
+                    p0 = proc.calc_probability(qstates, q)
+                    u = next(uniforms) if uniforms is not None else np.random.random_sample()
+                    v = 0 if u < p0 else 1
+                    proc.decohere(v, p0, qstates, q)
+                    lane_state[q] = v
+                    clbits[c] = v
+                    if v == 0:
+                        known_zero.add(q)
+                    else:
+                        known_zero.discard(q)
+                elif kind == 'r':
+                    q = it[1]
+                    v = lane_state.get(q, -1)
+                    if v == 1:
+                        proc.apply_reset(qstates, q)
+                        del lane_state[q]
+                    elif v == -1 and q not in known_zero:
+                        raise RuntimeError('Qubit is not measured.')
+                    known_zero.add(q)
+                elif kind == 'if':
+                    first, size, value, body = it[1:]
+                    reg = sum(clbits[first + k] << k for k in range(size))
+                    if reg == value:
+                        execute(body)
+
+        execute(prog)
+        for q in range(self.n_qubits):
+            if hasattr(qstates, 'set_lane_state'):
+                qstates.set_lane_state(q, lane_state.get(q, -1))
+        return sum(b << k for k, b in enumerate(clbits))
+
+    def _plan_host(self, items):
+        out, run = [], []
+        for it in items:
+            if it[0] == 'g':
+                run.append(it[1:])
+                continue
+            if run:
+                out.append(('h', None, list(run)))
+                run = []
+            if it[0] == 'if':
+                out.append(('if',) + it[1:4] + (self._plan_host(it[4]),))
+            else:
+                out.append(it)
+        if run:
+            out.append(('h', None, list(run)))
+        return out
+
+    def shots(self, rt, n_shots, dtype=np.float32, randnum=None, graph=True):
+        """Runs the program `n_shots` times from |0...0> on one states object
+        of the runtime `rt` (reset between shots) and returns the classical
+        registers (int64, bit j = classical bit j).  `randnum` supplies the
+        measurements' uniforms in order across all shots."""
+        qs = rt.create_qubit_states(dtype)
+        qs.processor.initialize_qubit_states(qs, self.n_qubits)
+        uniforms = iter(randnum) if randnum is not None else None
+        out = np.zeros(n_shots, np.int64)
+        try:
+            for k in range(n_shots):
+                qs.processor.reset_qubit_states(qs)
+                out[k] = self.run(qs, uniforms, graph=graph)
+        finally:
+            qs.delete()
+        return out
+
+    def delete(self):
+        """Frees the compiled segments built by run()."""
+        def free(items):
+            for it in items:
+                if it[0] == 'c':
+                    it[1].delete()
+                elif it[0] == 'if':
+                    free(it[4])
+        for prog in self._segments.values():
+            free(prog)
+        self._segments.clear()
 
     def gates(self):
         """The ops in the form CompiledCircuit and apply_controlled_gate take:
@@ -485,7 +688,8 @@ class QasmProgram:
         `qstates` (its state after the program ran), through the runtime's
         sampling pool over the measured lanes (the other lanes summed out).
         Returns int64 values with bit j = classical bit j; `randnum` are the
-        pool's uniforms (numpy's when None)."""
+        pool's uniforms (numpy's when None).  Static programs only."""
+        self._static_only('sample()')
         if not self.measurements:
             raise QasmError('the program measures nothing.')
         from .circuit import Lane
@@ -508,14 +712,16 @@ class QasmProgram:
         return out
 
     def compile(self, dtype=np.float32, graph=True):
-        """A CompiledCircuit of the program's gates (complex64 for float32)."""
+        """A CompiledCircuit of the program's gates (complex64 for float32).
+        Static programs only."""
+        self._static_only('compile()')
         from .compiled import CompiledCircuit
         return CompiledCircuit(dtype, self.gates(), graph=graph)
 
 
 def parse(text):
-    """Parses OpenQASM 2.0 source into a QasmProgram (QasmError on anything
-    the engine cannot run as a compiled circuit)."""
+    """Parses OpenQASM 2.0 source into a QasmProgram (QasmError on syntax
+    errors and on what the engine cannot run, such as opaque gates)."""
     return QasmProgram(_Parser(text).program())
 
 

@@ -152,10 +152,8 @@ def test_rzz_and_user_gate_nesting():
     ('OPENQASM 2.0; include "qelib1.inc"; qreg q[1]; cx q[0];', 'takes 0 parameters and 2'),
     ('OPENQASM 2.0; include "qelib1.inc"; qreg q[2]; cx q[0], q[0];', 'twice'),
     ('OPENQASM 2.0; include "qelib1.inc"; qreg q[2]; qreg r[3]; cx q, r;', 'different sizes'),
-    ('OPENQASM 2.0; include "qelib1.inc"; qreg q[1]; creg c[1]; measure q -> c; h q[0];',
-     'after its measurement'),
-    ('OPENQASM 2.0; include "qelib1.inc"; qreg q[1]; h q[0]; reset q[0];', 'reset'),
-    ('OPENQASM 2.0; qreg q[1]; creg c[1]; if (c == 1) U(0, 0, 0) q[0];', 'classically'),
+    ('OPENQASM 2.0; qreg q[1]; creg c[1]; if (d == 1) U(0, 0, 0) q[0];', 'unknown creg'),
+    ('OPENQASM 2.0; qreg q[1]; creg c[1]; if (c == 1) barrier q;', 'cannot follow if'),
     ('OPENQASM 2.0; opaque g q;', 'opaque'),
     ('OPENQASM 2.0; qreg q[1]; U(1/0, 0, 0) q[0];', 'division by zero'),
     ('OPENQASM 2.0; qreg q[1]; gate g x { U(t, 0, 0) x; } g q[0];', 'unknown parameter'),
@@ -255,3 +253,106 @@ def test_sample_maps_measured_lanes_to_classical_bits():
     assert 0.45 < np.mean(out == 0b101) < 0.55
     with pytest.raises(qasm.QasmError, match='measures nothing'):
         qasm.parse('OPENQASM 2.0; qreg q[1];').sample(_FakeRuntime(), qs, 1)
+
+
+# ------------------------------------------------------------------ dynamic programs
+
+class _OracleStates:
+    """A states object of the oracle runtime (oracle/runtime.py) with n lanes
+    in |0...0>."""
+
+    def __new__(cls, n):
+        from oracle.runtime import OracleQubitStates
+        qs = OracleQubitStates(np.float64)
+        qs.processor.initialize_qubit_states(qs, n)
+        qs.processor.reset_qubit_states(qs)
+        return qs
+
+
+def _oracle_gates(qs, gates):
+    for m, t, c in gates:
+        if c:
+            sv.apply_controlled_gate(qs.psi, m, list(c), t)
+        else:
+            sv.apply_gate(qs.psi, m, t)
+
+
+TELEPORT = ('OPENQASM 2.0; include "qelib1.inc"; qreg q[3]; creg a[1]; creg b[1]; '
+            'u3(0.7, 0.4, -1.1) q[0]; h q[1]; cx q[1], q[2]; cx q[0], q[1]; h q[0]; '
+            'measure q[0] -> a[0]; measure q[1] -> b[0]; '
+            'if (b == 1) x q[2]; if (a == 1) z q[2];')
+
+
+def test_dynamic_program_items():
+    p = qasm.parse(TELEPORT)
+    assert p.dynamic
+    kinds = [it[0] for it in p.items]
+    assert kinds == ['g'] * 5 + ['m', 'm', 'if', 'if']
+    assert p.items[7][1:4] == (1, 1, 1) and p.items[7][4][0][0] == 'g'
+    with pytest.raises(qasm.QasmError, match='run it shot by shot'):
+        p.compile()
+    static = qasm.parse('OPENQASM 2.0; include "qelib1.inc"; qreg q[2]; creg c[2]; reset q; '
+                        'h q[0]; measure q -> c;')
+    assert not static.dynamic
+
+
+@pytest.mark.parametrize('u', [(0.1, 0.1), (0.1, 0.9), (0.9, 0.1), (0.9, 0.9)])
+def test_teleportation_every_branch(u):
+    """Whatever the two outcomes, q[2] ends in the state q[0] started in."""
+    p = qasm.parse(TELEPORT)
+    qs = _OracleStates(3)
+    bits = p.run(qs, randnum=list(u), gate_runner=_oracle_gates)
+    psi = qs.psi.reshape(2, 2, 2)  # [q2, q1, q0]
+    a, b = bits & 1, bits >> 1 & 1
+    assert (qs.get_lane_state(0), qs.get_lane_state(1)) == (a, b)
+    q2 = psi[:, b, a]
+    want = qasm._u(0.7, 0.4, -1.1) @ np.array([1, 0])
+    assert abs(abs(np.vdot(want, q2)) - 1.) < 1e-12
+
+
+def test_measurement_follows_the_reference_rule():
+    """outcome 0 iff u < Pr(q = 0); the state collapses; a reset of a qubit
+    measured 1 brings it back to |0>."""
+    p = qasm.parse('OPENQASM 2.0; include "qelib1.inc"; qreg q[1]; creg c[1]; '
+                   'ry(1.0) q[0]; measure q[0] -> c[0]; reset q[0]; measure q[0] -> c[0];')
+    p0 = math.cos(0.5) ** 2
+    for u, first in ((p0 - 1e-9, 0), (p0 + 1e-9, 1)):
+        qs = _OracleStates(1)
+        bits = []
+        orig = qs.processor.decohere
+
+        def record(v, prob, q, lane, orig=orig):
+            bits.append(v)
+            return orig(v, prob, q, lane)
+        qs.processor.decohere = record
+        out = p.run(qs, randnum=[u, 0.5], gate_runner=_oracle_gates)
+        assert bits == [first, 0] and out == 0
+        assert np.allclose(qs.psi, [1, 0])
+
+
+def test_reset_needs_a_measured_or_fresh_qubit():
+    ok = qasm.parse('OPENQASM 2.0; include "qelib1.inc"; qreg q[2]; creg c[1]; reset q[1]; '
+                    'x q[0]; measure q[0] -> c[0]; reset q[0]; reset q[0];')
+    qs = _OracleStates(2)
+    assert ok.run(qs, randnum=[0.5], gate_runner=_oracle_gates) == 1
+    assert np.allclose(qs.psi, [1, 0, 0, 0])
+    bad = qasm.parse('OPENQASM 2.0; include "qelib1.inc"; qreg q[1]; h q[0]; reset q[0];')
+    with pytest.raises(RuntimeError, match='not measured'):
+        bad.run(_OracleStates(1), gate_runner=_oracle_gates)
+    # a gate on a measured qubit makes it unmeasured again
+    stale = qasm.parse('OPENQASM 2.0; include "qelib1.inc"; qreg q[1]; creg c[1]; x q[0]; '
+                       'measure q[0] -> c[0]; h q[0]; reset q[0];')
+    with pytest.raises(RuntimeError, match='not measured'):
+        stale.run(_OracleStates(1), randnum=[0.5], gate_runner=_oracle_gates)
+
+
+def test_if_compares_the_whole_register():
+    src = ('OPENQASM 2.0; include "qelib1.inc"; qreg q[3]; creg c[2]; x q[1]; '
+           'measure q[0] -> c[0]; measure q[1] -> c[1]; '
+           'if (c == 2) x q[2]; if (c == 1) h q[2]; if (c == 3) y q[2];')
+    p = qasm.parse(src)
+    qs = _OracleStates(3)
+    assert p.run(qs, randnum=[0.5, 0.5], gate_runner=_oracle_gates) == 2
+    want = np.zeros(8)
+    want[0b110] = 1
+    assert np.allclose(qs.psi, want)

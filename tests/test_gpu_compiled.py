@@ -164,3 +164,55 @@ def test_qasm_programs_as_compiled_circuits(rt, dtype):
             got = _state(qs)
             qs.delete()
         assert np.allclose(got, want, atol=ATOL[dtype] * 8)
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_qasm_dynamic_programs_shot_by_shot(rt, dtype):
+    """OpenQASM programs with mid-circuit measurements, resets and if (run
+    shot by shot: compiled gate segments, the runtime's decohere / reset /
+    calc_probability between them) against the same programs on the oracle
+    runtime with the same uniforms: equal classical registers and states.
+    A 12-qubit program interleaving random layers with measure / if / reset
+    on a few qubits, and teleportation on every branch."""
+    from oracle.runtime import OracleQubitStates
+    from qgate_gb300 import qasm
+    rng = np.random.default_rng(8)
+    n = 12
+    lines = ['OPENQASM 2.0;', 'include "qelib1.inc";', 'qreg q[%d];' % n, 'creg c[3];']
+    for layer in range(4):
+        for q in range(n):
+            a, b, g = rng.uniform(0, 2 * np.pi, 3)
+            lines.append('u3(%r, %r, %r) q[%d];' % (a, b, g, q))
+        for k in range(0, n - 1, 2):
+            lines.append('cx q[%d], q[%d];' % (k + layer % 2, (k + 1 + layer % 2) % n))
+        m = int(rng.integers(n))
+        lines.append('measure q[%d] -> c[%d];' % (m, layer % 3))
+        lines.append('if (c == %d) h q[%d];' % (layer % 4, (m + 5) % n))
+        lines.append('reset q[%d];' % m)
+    lines.append('measure q[0] -> c[0]; measure q[1] -> c[1]; measure q[2] -> c[2];')
+    progs = ['\n'.join(lines),
+             'OPENQASM 2.0; include "qelib1.inc"; qreg q[3]; creg a[1]; creg b[1]; '
+             'u3(0.7, 0.4, -1.1) q[0]; h q[1]; cx q[1], q[2]; cx q[0], q[1]; h q[0]; '
+             'measure q[0] -> a[0]; measure q[1] -> b[0]; if (b == 1) x q[2]; '
+             'if (a == 1) z q[2];']
+
+    def oracle_gates(qs, gates):
+        for mat, t, c in gates:
+            sv.apply_controlled_gate(qs.psi, mat, list(c), t)
+
+    for src in progs:
+        prog = qasm.parse(src)
+        assert prog.dynamic
+        for trial in range(4):
+            u = np.random.default_rng(100 + trial).random(16)
+            ref = OracleQubitStates(np.float64)
+            ref.processor.initialize_qubit_states(ref, prog.n_qubits)
+            ref.processor.reset_qubit_states(ref)
+            want_bits = prog.run(ref, randnum=u, gate_runner=oracle_gates)
+            qs = new_state(rt, prog.n_qubits, dtype)
+            got_bits = prog.run(qs, randnum=u, graph=trial % 2 == 1)
+            got = _state(qs)
+            qs.delete()
+            assert got_bits == want_bits, (src[:40], trial)
+            assert np.allclose(got, ref.psi, atol=ATOL[dtype] * 8), (src[:40], trial)
+        prog.delete()
