@@ -181,7 +181,7 @@ def test_qasm_dynamic_programs_shot_by_shot(rt, dtype):
     lines = ['OPENQASM 2.0;', 'include "qelib1.inc";', 'qreg q[%d];' % n, 'creg c[3];']
     for layer in range(4):
         for q in range(n):
-            a, b, g = rng.uniform(0, 2 * np.pi, 3)
+            a, b, g = (float(x) for x in rng.uniform(0, 2 * np.pi, 3))
             lines.append('u3(%r, %r, %r) q[%d];' % (a, b, g, q))
         for k in range(0, n - 1, 2):
             lines.append('cx q[%d], q[%d];' % (k + layer % 2, (k + 1 + layer % 2) % n))
