@@ -326,20 +326,18 @@ void build_launches(const std::vector<Op> &ops, const std::vector<int> &order, i
 struct TcForward {
     struct Step {
         TcStageDesc desc;     // bmats filled at launch
-        size_t ops_off;       // FP16 offset of batch element 0's operands
-        size_t ops_stride;    // FP16 per batch element
+        size_t ops_off;       // byte offset of batch element 0's operands
+        size_t ops_stride;    // operand bytes per batch element
         int ckpt_after;       // save psi to this checkpoint after the step (-1: none)
     };
     std::vector<Step> steps;
-    std::vector<unsigned short> ops;  // [step][batch][nb][Bh | Bl]
+    std::vector<unsigned char> ops;  // [step][batch][nb][Bh | Bl]
 };
 
 void plan_tc_forward(const std::vector<Op> &ops, const std::vector<int> &bounds, int n, int batch,
                      int n_params, const double *params, TcForward &out) {
     const int M = 12;
     const unsigned long long base = (1ULL << 4) - 1;
-    const size_t kBlockHalves = 2 * 64 * 64;
-    const int per_launch = tstage_max_blocks(M);
     auto gate_of = [&](const Op &o, int b) {
         PendingGate g;
         g.target = o.target;
@@ -372,11 +370,14 @@ void plan_tc_forward(const std::vector<Op> &ops, const std::vector<int> &bounds,
                 for (auto *g : bl.second) ix.push_back((int)(g - g0.data()));
                 bidx.emplace_back(bl.first, ix);
             }
-            for (size_t b0 = 0; b0 < bidx.size(); b0 += per_launch) {
-                const int nb = (int)std::min<size_t>(per_launch, bidx.size() - b0);
+            // dense ops only: whether a rotation is diagonal depends on its
+            // angle, which differs between parameter vectors
+            const TcOps ops0 = tc_ops(blocks0, false);
+            for (size_t b0 = 0; b0 < bidx.size();) {
+                const int nb = tc_ops_per_launch(ops0, b0);
                 TcForward::Step st;
                 st.ops_off = out.ops.size();
-                st.ops_stride = nb * kBlockHalves;
+                st.ops_stride = (size_t)nb * tc_op_bytes(ops0[b0]);
                 st.ckpt_after = -1;
                 out.ops.resize(out.ops.size() + (size_t)batch * st.ops_stride);
                 std::vector<TcStageDesc> descs(batch);
@@ -391,11 +392,12 @@ void plan_tc_forward(const std::vector<Op> &ops, const std::vector<int> &bounds,
                         for (int ix : bi.second) ptrs.push_back(&gb[ix]);
                         blocks.emplace_back(bi.first, ptrs);
                     }
-                    tc_plan_launch(tl, n, blocks, b0, nb, descs[b],
+                    tc_plan_launch(tl, n, tc_ops(blocks, false), b0, nb, descs[b],
                                    out.ops.data() + st.ops_off + (size_t)b * st.ops_stride);
                 }
                 st.desc = descs[0];
                 out.steps.push_back(st);
+                b0 += nb;
             }
             remaining.swap(deferred);
         }
@@ -506,9 +508,8 @@ static void adjoint_run(int prec, int n, std::vector<Op> &ops, const double *par
             launch_init_basis(prec, (char *)psi + state_bytes * b, (idx_t)1 << n, st);
 
         if (tc_fwd) {
-            unsigned short *dops = (unsigned short *)alloc(
-                std::max<size_t>(tcf.ops.size() * sizeof(unsigned short), 16));
-            QG_CUDA(cudaMemcpyAsync(dops, tcf.ops.data(), tcf.ops.size() * sizeof(unsigned short),
+            unsigned char *dops = (unsigned char *)alloc(std::max<size_t>(tcf.ops.size(), 16));
+            QG_CUDA(cudaMemcpyAsync(dops, tcf.ops.data(), tcf.ops.size(),
                                     cudaMemcpyHostToDevice, st));
             for (auto &step : tcf.steps) {
                 TcStageDesc d = step.desc;

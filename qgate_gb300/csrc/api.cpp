@@ -152,7 +152,7 @@ struct Circuit {
     unsigned version = 0;
     long long passes = 0, bytes = 0;
     static constexpr size_t kChunkBytes = 8ull << 20;
-    std::vector<std::pair<unsigned short *, unsigned short *>> chunks;
+    std::vector<std::pair<unsigned char *, unsigned char *>> chunks;
     size_t chunk_off = 0;
 };
 
@@ -195,7 +195,7 @@ struct Device {
     bool tensor_blocks = true;
     // Ring of split block operands: pinned host staging and its device copy.
     static constexpr size_t kBRingBytes = 32ull << 20;
-    unsigned short *h_bring = nullptr, *d_bring = nullptr;
+    unsigned char *h_bring = nullptr, *d_bring = nullptr;
     size_t bring_off = 0;
     long long n_gates = 0, n_passes = 0, n_bytes = 0;
     // Per-kernel-class launch timing with CUDA events on the engine's stream.
@@ -512,24 +512,22 @@ static bool schedule_rstage(const std::vector<const PendingGate *> &gates, const
 static void run_tstage(Device &d, States *s, const TileLanes &tl,
                        const std::vector<const PendingGate *> &gates) {
     const int n = s->n_lanes;
-    const int m = (int)tl.lanes.size();
-    auto blocks = tc_blocks(gates, tl);
+    const TcOps ops = tc_ops(tc_blocks(gates, tl), true);
     if (!d.h_bring) {
         QG_CUDA(cudaMallocHost(&d.h_bring, Device::kBRingBytes));
         QG_CUDA(cudaMalloc(&d.d_bring, Device::kBRingBytes));
         d.bring_off = 0;
     }
-    const size_t kBlockHalves = 2 * 64 * 64;
-    const size_t per_launch = (size_t)tstage_max_blocks(m);
-    for (size_t b0 = 0; b0 < blocks.size(); b0 += per_launch) {
-        const int nb = (int)std::min<size_t>(per_launch, blocks.size() - b0);
-        const size_t bytes = nb * kBlockHalves * sizeof(unsigned short);
-        unsigned short *hb, *db;
+    for (size_t b0 = 0; b0 < ops.size();) {
+        const int nb = tc_ops_per_launch(ops, b0);
+        size_t bytes = 0;
+        for (int b = 0; b < nb; ++b) bytes += tc_op_bytes(ops[b0 + b]);
+        unsigned char *hb, *db;
         if (d.capturing) {
             // operands a captured graph re-reads: chunks owned by the circuit
             Circuit *c = d.capturing;
             if (c->chunks.empty() || c->chunk_off + bytes > Circuit::kChunkBytes) {
-                unsigned short *h = nullptr, *dv = nullptr;
+                unsigned char *h = nullptr, *dv = nullptr;
                 QG_CUDA(cudaMallocHost(&h, Circuit::kChunkBytes));
                 if (cudaMalloc(&dv, Circuit::kChunkBytes) != cudaSuccess) {
                     cudaFreeHost(h);
@@ -538,31 +536,29 @@ static void run_tstage(Device &d, States *s, const TileLanes &tl,
                 c->chunks.emplace_back(h, dv);
                 c->chunk_off = 0;
             }
-            hb = c->chunks.back().first + c->chunk_off / sizeof(unsigned short);
-            db = c->chunks.back().second + c->chunk_off / sizeof(unsigned short);
+            hb = c->chunks.back().first + c->chunk_off;
+            db = c->chunks.back().second + c->chunk_off;
             c->chunk_off += bytes;
         } else {
             if (d.bring_off + bytes > Device::kBRingBytes) {
                 QG_CUDA(cudaStreamSynchronize(d.stream));  // the staging is reused
                 d.bring_off = 0;
             }
-            hb = d.h_bring + d.bring_off / sizeof(unsigned short);
-            db = d.d_bring + d.bring_off / sizeof(unsigned short);
+            hb = d.h_bring + d.bring_off;
+            db = d.d_bring + d.bring_off;
             d.bring_off += bytes;
         }
         static TcStageDesc desc;
-        tc_plan_launch(tl, n, blocks, b0, nb, desc, hb);
+        tc_plan_launch(tl, n, ops, b0, nb, desc, hb);
         desc.bmats = db;
         QG_CUDA(cudaMemcpyAsync(db, hb, bytes, cudaMemcpyHostToDevice, d.stream));
         timed(d, "tstage", [&] { launch_tstage(s->d, desc, d.stream, d.pipelined); });
         d.n_passes += 1;
         d.n_bytes += 2 * ((long long)1 << n) * (long long)complex_size(s->prec);
+        b0 += nb;
     }
 }
 
-// complex128 register stages compute in double-float: each FP64 matrix
-// entry of an op is packed as its (h, l) FP32 pair, h = fl32(v), l =
-// fl32(v - h), in the entry's own 8-byte slot.
 static void pack_double_float(RStageDesc<double> &desc) {
     for (int i = 0; i < desc.nops; ++i) {
         RegOp<double> &o = desc.ops[i];

@@ -137,14 +137,18 @@ template <class R> struct RStageDesc {
     RegOp<R> ops[kMaxRegOps];                     // 16-byte aligned
 };
 
-// Tensor-core stage (complex64): fused 5-lane blocks applied as tcgen05
-// products to a tile of m = 12 or 13 lanes.  Load layout: thread bit b holds
-// global lane row_lane[b], register bit k global lane log2(dep_hi[1 << k]).
-// sets[b] maps the registers of the layout before block b (the load layout
-// for b = 0) to the slots of block b's operand layout; sets[nblocks] maps the
-// last block's layout, sets[nblocks + 1] the load layout, to the swizzled
-// natural tile.  bmats holds per block the split operands Bh, Bl (2 x 4096
-// FP16 values, canonical K-major layout).
+// Tensor-core stage (complex64): a sequence of ops on a tile of m = 12 or 13
+// lanes - fused 5-lane blocks applied as tcgen05 products (dense ops) and
+// diagonal phase tables applied elementwise (phase ops).  Load layout:
+// thread bit b holds global lane row_lane[b], register bit k global lane
+// log2(dep_hi[1 << k]).  sets[b] maps the registers of the layout before op
+// b (the load layout for b = 0) to the slots of dense op b's operand layout,
+// or to the entries of phase op b's table (a phase op keeps the layout);
+// sets[nblocks] maps the layout after the last op, sets[nblocks + 1] the load
+// layout, to the swizzled natural tile.  bmats holds the ops' operands, op b
+// at byte op_off[b]: a dense op's split operands Bh, Bl (2 x 4096 FP16
+// values, canonical K-major layout), a phase op's table of complex64 phases
+// (ops_bytes in all, a multiple of 16).
 constexpr int kMaxTcBlocks = 24;
 struct TcStageDesc {
     int n, m;
@@ -152,15 +156,17 @@ struct TcStageDesc {
     int nins;
     int ins_pos[kMaxTileLanes];
     long long dep_hi[32];
-    int nblocks;
-    const unsigned short *bmats;
+    long long in_e[5];                    // dep_hi[1 << k]
+    int nblocks;                          // ops
+    unsigned ops_bytes;
+    unsigned op_off[kMaxTcBlocks];        // byte offset of op b's operands
+    unsigned char op_kind[kMaxTcBlocks];  // 0: dense block, 1: phase table
+    const unsigned char *bmats;
     SetSlots sets[kMaxTcBlocks + 2];
 };
 // two_per_row: the 12-lane variant with two threads per tile row (twice the
 // warps per SM, half the registers per thread).
 void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool two_per_row);
-// Blocks one tensor-stage launch holds (its operands stay in shared memory).
-int tstage_max_blocks(int m);
 // Status word of the tensor stage kernels (nonzero: a bounded wait gave up).
 int tstage_status(bool reset);
 

@@ -42,11 +42,29 @@ unsigned long long plan_stage_lanes(const std::vector<const PendingGate *> &rema
 typedef std::vector<std::pair<unsigned, std::vector<const PendingGate *>>> TcBlocks;
 TcBlocks tc_blocks(const std::vector<const PendingGate *> &gates, const TileLanes &tl);
 
-// Host plan of one tensor-stage launch over blocks [b0, b0 + nb): the
-// descriptor (all but the operand pointer) and the split block operands
-// (nb x 2 x 4096 FP16 values) in `ops`.
-void tc_plan_launch(const TileLanes &tl, int n, const TcBlocks &blocks, size_t b0, int nb,
-                    TcStageDesc &desc, unsigned short *ops);
+// Ops of a tensor stage: each fused block is a dense op (a 32x32 unitary on
+// the tensor cores); with `phases`, every run of consecutive blocks whose
+// gates are all diagonal becomes one phase op instead (their product, a
+// diagonal over the union of their lanes, applied elementwise).
+struct TcOp {
+    bool phase;
+    unsigned lanes;  // tile-position mask
+    std::vector<const PendingGate *> gates;
+};
+typedef std::vector<TcOp> TcOps;
+TcOps tc_ops(const TcBlocks &blocks, bool phases);
+// Operand bytes of an op: 16 KB for a dense op (Bh, Bl), 8 bytes per entry of
+// a phase table (2^lanes complex64 phases).
+size_t tc_op_bytes(const TcOp &op);
+// How many ops from ops[b0] one launch holds (their operands and slot tables
+// in the shared memory a tensor-stage launch leaves for them).
+int tc_ops_per_launch(const TcOps &ops, size_t b0);
+
+// Host plan of one tensor-stage launch over ops [b0, b0 + nb): the
+// descriptor (all but the operand pointer) and the ops' operands in `buf`
+// (dense ops first, then the phase tables; desc.ops_bytes in all).
+void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int nb,
+                    TcStageDesc &desc, unsigned char *buf);
 
 // Whether complex64 stages run on the tensor cores (the gate queue's setting).
 bool tensor_stages_enabled();

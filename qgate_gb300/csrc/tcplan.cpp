@@ -442,23 +442,111 @@ static int tc_store_cost8(const SetSlots &ss) {
     return cost;
 }
 
-// Host plan of one tensor-stage launch: blocks [b0, b0 + nb) of a stage on
-// tile `tl` -> the descriptor (all but the operand pointer) and the split
-// block operands (nb x 2 x 4096 FP16 values) in `ops`.
-void tc_plan_launch(const TileLanes &tl, int n, const TcBlocks &blocks, size_t b0, int nb,
-                    TcStageDesc &desc, unsigned short *ops) {
+// ---------------------------------------------------------------- stage ops
+
+TcOps tc_ops(const TcBlocks &blocks, bool phases) {
+    TcOps out;
+    for (const auto &bl : blocks) {
+        bool diag = phases;
+        for (auto *g : bl.second) diag = diag && g->diag;
+        if (diag && !out.empty() && out.back().phase) {
+            out.back().lanes |= bl.first;
+            out.back().gates.insert(out.back().gates.end(), bl.second.begin(), bl.second.end());
+            continue;
+        }
+        TcOp op;
+        op.phase = diag;
+        op.lanes = bl.first;
+        op.gates = bl.second;
+        out.push_back(std::move(op));
+    }
+    return out;
+}
+
+size_t tc_op_bytes(const TcOp &op) {
+    return op.phase ? (size_t)8 << __builtin_popcount(op.lanes) : (size_t)2 * 64 * 64 * 2;
+}
+
+// Shared memory a launch has for its ops' operands and slot tables: the
+// opt-in maximum (227 KB) less 2 KB of static shared memory, 128 KB of tile
+// operands (4 groups x 2 x 16 KB for 12-lane tiles, 2 x 2 x 32 KB for 13-lane
+// tiles; 3 groups of the two-threads-per-row variant take less) and the two
+// natural-tile slot tables.
+constexpr size_t kTcOpsBudget = 227 * 1024 - 2048 - 128 * 1024 - 2 * sizeof(SetSlots);
+
+int tc_ops_per_launch(const TcOps &ops, size_t b0) {
+    size_t used = 0;
+    int nb = 0;
+    while (b0 + nb < ops.size() && nb < kMaxTcBlocks) {
+        const size_t add = tc_op_bytes(ops[b0 + nb]) + sizeof(SetSlots);
+        if (nb > 0 && used + add > kTcOpsBudget) break;
+        used += add;
+        ++nb;
+    }
+    return nb;
+}
+
+// Table of a phase op: entry idx (bit k of idx = tile position order[k]) is
+// the product of the op's diagonal gates' entries at that assignment of
+// their lanes (m00 or m11 of a gate whose controls are all set, else 1),
+// computed in FP64 and rounded to complex64.
+static void tc_phase_table(const TcOp &op, const TileLanes &tl, const std::vector<int> &order,
+                           float *table) {
+    typedef std::complex<double> cd;
+    const int u = (int)order.size();
+    int bit_of[64];
+    for (int p = 0; p < 64; ++p) bit_of[p] = -1;
+    for (int k = 0; k < u; ++k) bit_of[order[k]] = k;
+    for (unsigned idx = 0; idx < (1u << u); ++idx) {
+        cd ph(1., 0.);
+        for (auto *g : op.gates) {
+            bool on = true;
+            for (int c : g->controls) on = on && (idx >> bit_of[tl.local_of[c]] & 1u);
+            if (!on) continue;
+            ph *= (idx >> bit_of[tl.local_of[g->target]] & 1u) ? cd(g->m.v[6], g->m.v[7])
+                                                               : cd(g->m.v[0], g->m.v[1]);
+        }
+        table[2 * idx] = (float)ph.real();
+        table[2 * idx + 1] = (float)ph.imag();
+    }
+}
+
+// Host plan of one tensor-stage launch: ops [b0, b0 + nb) of a stage on tile
+// `tl` -> the descriptor (all but the operand pointer) and the ops' operands
+// in `buf`.
+void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int nb,
+                    TcStageDesc &desc, unsigned char *buf) {
     const int m = (int)tl.lanes.size();
     const int t = m - 5;
-    const size_t kBlockHalves = 2 * 64 * 64;
     memset(&desc, 0, sizeof(desc));
     desc.n = n;
     desc.m = m;
     desc.nins = m < n ? m : 0;
     for (int j = 0; j < desc.nins; ++j) desc.ins_pos[j] = tl.lanes[j];
     desc.nblocks = nb;
+    {
+        // operand offsets: dense ops first (16 KB each), then the phase tables
+        unsigned off = 0;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int b = 0; b < nb; ++b)
+                if (ops[b0 + b].phase == (pass == 1)) {
+                    desc.op_off[b] = off;
+                    off += (unsigned)tc_op_bytes(ops[b0 + b]);
+                }
+        desc.ops_bytes = off;
+    }
+    auto next_dense = [&](int b) -> int {
+        for (int x = b + 1; x < nb; ++x)
+            if (!ops[b0 + x].phase) return x;
+        return -1;
+    };
+    const int first_dense = ops[b0].phase ? next_dense(0) : 0;
+    int last_dense = -1;
+    for (int b = 0; b < nb; ++b)
+        if (!ops[b0 + b].phase) last_dense = b;
     // Load layout: tile positions 0..3 (the contiguous low lanes) plus one
     // more position p on the warp's thread bits, chosen so that the first
-    // block's operand stores hit the fewest banks twice.
+    // dense op's operand stores hit the fewest banks twice.
     auto load_layout = [&](int p) {
         TcLayout L;
         for (int i = 0; i < 8; ++i) L.rows[i] = -1;
@@ -473,22 +561,20 @@ void tc_plan_launch(const TileLanes &tl, int n, const TcBlocks &blocks, size_t b
         return L;
     };
     TcLayout cur = load_layout(4);
-    {
-        unsigned lanes0 = tc_fill_lanes(blocks[b0].first, cur, m);
-        const unsigned next0 = nb > 1 ? blocks[b0 + 1].first : 0u;
+    if (first_dense >= 0) {
+        const int nd = next_dense(first_dense);
+        const unsigned next0 = nd >= 0 ? ops[b0 + nd].lanes : 0u;
         int best = 1 << 30;
         for (int p = 4; p < m; ++p) {
             TcLayout L = load_layout(p);
-            unsigned l0 = tc_fill_lanes(blocks[b0].first, L, m);
+            unsigned l0 = tc_fill_lanes(ops[b0 + first_dense].lanes, L, m);
             TcLayout lay = tc_choose_layout(l0, next0, L, m);
             int c = tc_store_cost(tc_slots(L, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); }));
             if (c < best) {
                 best = c;
                 cur = L;
-                lanes0 = l0;
             }
         }
-        (void)lanes0;
     }
     for (int b = 0; b < t; ++b) desc.row_lane[b] = tl.lanes[cur.rows[b]];
     for (int j = 0; j < 32; ++j) {
@@ -497,15 +583,36 @@ void tc_plan_launch(const TileLanes &tl, int n, const TcBlocks &blocks, size_t b
             if (j >> k & 1) off |= 1LL << tl.lanes[cur.amps[k]];
         desc.dep_hi[j] = off;
     }
+    for (int k = 0; k < 5; ++k) desc.in_e[k] = desc.dep_hi[1 << k];
     desc.sets[nb + 1] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
     std::complex<double> U[1024];
     for (int b = 0; b < nb; ++b) {
-        unsigned lanes = blocks[b0 + b].first;
-        lanes = tc_fill_lanes(lanes, cur, m);
-        const unsigned next = b + 1 < nb ? blocks[b0 + b + 1].first : 0u;
+        const TcOp &op = ops[b0 + b];
+        if (op.phase) {
+            // table index bits: the op's lanes on the warp's thread bits
+            // first (a warp then reads few distinct banks), then the others
+            std::vector<int> order;
+            for (int x = 0; x < 5; ++x)
+                if (op.lanes >> cur.rows[x] & 1u) order.push_back(cur.rows[x]);
+            for (int p = 0; p < m; ++p)
+                if ((op.lanes >> p & 1u) && std::find(order.begin(), order.end(), p) == order.end())
+                    order.push_back(p);
+            desc.op_kind[b] = 1;
+            desc.sets[b] = tc_slots(cur, t, [&](unsigned ti) {
+                unsigned idx = 0;
+                for (size_t k = 0; k < order.size(); ++k)
+                    if (ti >> order[k] & 1u) idx |= 1u << k;
+                return idx;
+            });
+            tc_phase_table(op, tl, order, (float *)(buf + desc.op_off[b]));
+            continue;
+        }
+        unsigned lanes = tc_fill_lanes(op.lanes, cur, m);
+        const int nd = next_dense(b);
+        const unsigned next = nd >= 0 ? ops[b0 + nd].lanes : 0u;
         TcLayout lay = tc_choose_layout(lanes, next, cur, m);
-        if (b + 1 == nb) {
-            // Last block: rows[3..4] only feed the 8-byte stores into the
+        if (b == last_dense) {
+            // Last dense op: rows[3..4] only feed the 8-byte stores into the
             // natural tile; pick them for the fewest wavefronts there.
             int best = 1 << 30;
             TcLayout keep = lay;
@@ -523,10 +630,12 @@ void tc_plan_launch(const TileLanes &tl, int n, const TcBlocks &blocks, size_t b
                     }
                 }
         }
+        desc.op_kind[b] = 0;
         desc.sets[b] = tc_slots(cur, t, [&](unsigned ti) { return tc_operand_slot(lay, ti); });
-        tc_block_matrix(blocks[b0 + b].second, tl, lay, U);
+        tc_block_matrix(op.gates, tl, lay, U);
         tc_compensate(U);
-        tc_operand(U, ops + b * kBlockHalves, ops + b * kBlockHalves + kBlockHalves / 2);
+        unsigned short *o = (unsigned short *)(buf + desc.op_off[b]);
+        tc_operand(U, o, o + 64 * 64);
         cur = lay;
     }
     desc.sets[nb] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });

@@ -172,10 +172,11 @@ __device__ __forceinline__ void group_sync(unsigned id, unsigned threads) {
 // and products on the SM's tensor core.  RT = 128-row groups per tile (tile
 // lanes m = 12 for RT = 1, 13 for RT = 2); H = threads per row (each thread
 // holds 32 / H amplitudes of its row; H = 2 halves the registers per thread
-// so that twice the warps fit).
-template <int RT, int G, int H>
+// so that twice the warps fit); PH = the launch has phase ops (without them
+// the kernel keeps the registers of the dense path alone).
+template <int RT, int G, int H, bool PH>
 __global__ void __launch_bounds__(128 * RT * G * H, 1)
-k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long long tiles) {
+k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tiles) {
     constexpr int m = RT == 1 ? 12 : 13;
     constexpr int t = m - 5;
     constexpr int NA = 32 / H;                          // amplitudes per thread
@@ -186,13 +187,13 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
     constexpr unsigned kColsGroup = 64u * RT;
     constexpr unsigned kCols = kColsGroup * G <= 32 ? 32 : (kColsGroup * G <= 64 ? 64 :
                                (kColsGroup * G <= 128 ? 128 : (kColsGroup * G <= 256 ? 256 : 512)));
-    constexpr unsigned kBBytes = 2u * 64u * 64u * 2u;   // Bh, Bl of one block in FP16
+    constexpr unsigned kBBytes = 2u * 64u * 64u * 2u;   // Bh, Bl of one dense op in FP16
     constexpr unsigned kABytes = 4u << m;               // one FP16 operand of a tile
     static_assert(H == 1 || H == 2, "threads per row");
     extern __shared__ __align__(1024) unsigned char smraw[];
     const int nb = d.nblocks;
-    unsigned char *Bs = smraw + (size_t)G * 2 * kABytes;
-    SetSlots *sset = (SetSlots *)(Bs + (size_t)nb * kBBytes);
+    unsigned char *Bs = smraw + (size_t)G * 2 * kABytes;  // the ops' operands
+    SetSlots *sset = (SetSlots *)(Bs + d.ops_bytes);
     __shared__ __align__(8) unsigned long long bar_mma[G], bar_b;
     __shared__ unsigned tmem_sh;
     __shared__ int abort_sh[G];
@@ -239,62 +240,67 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
     const unsigned tmem = tmem_sh + g * kColsGroup + 64u * (wg >> 2) + 32u * hh +
                           ((32u * (wg & 3u)) << 16);
     const unsigned dcol0 = tmem_sh + g * kColsGroup;       // the group's accumulator
-    if (tid == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bb),
-                     "r"((unsigned)nb * kBBytes)
-                     : "memory");
-        for (int b = 0; b < nb; ++b)
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-                "[%3];\n" ::"r"(smem_u32(Bs + (size_t)b * kBBytes)),
-                "l"(d.bmats + (size_t)b * (kBBytes / 2)), "r"(kBBytes), "r"(bb)
-                : "memory");
-    }
+    if (tid == 0) bulk_load(smem_u32(Bs), d.bmats, d.ops_bytes, bb);
 
     // Load layout: row bit b at global lane row_lane[b], amplitude bit k at
     // the lane of e[k] (chosen per stage on the host; lanes 0..3 of the tile
     // are among the warp's row bits, so accesses come in 128-byte runs).  A
     // thread holds amplitudes hh * NA + j of its row, j < NA.
-    long long e[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) e[k] = d.dep_hi[1 << k];
-    idx_t dt = 0;
-    for (int b = 0; b < t; ++b)
-        if (r & (1u << b)) dt |= 1LL << d.row_lane[b];
-    if (H == 2 && hh) dt += e[4];
-    // Slots of the load layout in the swizzled natural tile (copy-out).
-    const SetSlots &nat = sset[nb + 1];
-    unsigned pt = (unsigned)nat.lo[r & 31u] ^ (unsigned)nat.hi[r >> 5];
-    if (H == 2 && hh) pt ^= nat.q[4];
-    unsigned qn[NB];
-#pragma unroll
-    for (int k = 0; k < NB; ++k) qn[k] = nat.q[k];
+    const long long(&e)[5] = d.in_e;  // read from the parameter space where used
+    // This thread's row offset in the load layout (recomputed where used,
+    // which keeps it out of the registers the ops need).
+    auto row_offset = [&]() {
+        idx_t o = 0;
+        for (int b = 0; b < t; ++b)
+            if (r & (1u << b)) o |= 1LL << d.row_lane[b];
+        if (H == 2 && hh) o += e[4];
+        return o;
+    };
     const unsigned gbar = 1u + g;                          // the group's named barrier
     unsigned phase = 0;
-    bool ok = true, b_ready = false;
-    const long long tstep = (long long)gridDim.x * G;
+    bool ok = true, b_ready = false, t_ready = false;
+    const int tstep = (int)gridDim.x * G;
 
     // The next tile's loads are issued into v once the finished tile has
     // been staged in shared memory, before it is copied out, so they are in
     // flight during the copy-out; the scale is applied after.
     unsigned v[2 * NA];  // floats (bits): this thread's part of row r
-    auto load_raw = [&](long long tl) {
-        const float2 *gp0 = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
+    auto load_raw = [&](int tl) {
+        const float2 *gp0 = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | row_offset());
         gray_walk<NB>(gp0, e, [&](int j, const float2 *p) {
             const float2 x = *p;
             v[2 * j] = __float_as_uint(x.x);
             v[2 * j + 1] = __float_as_uint(x.y);
         });
     };
-    if ((long long)blockIdx.x * G + g < tiles) load_raw((long long)blockIdx.x * G + g);
-    for (long long tl = (long long)blockIdx.x * G + g; tl < tiles && ok; tl += tstep) {
-        float2 *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | dt);
+    if ((int)blockIdx.x * G + (int)g < tiles) load_raw((int)blockIdx.x * G + (int)g);
+    for (int tl = (int)blockIdx.x * G + (int)g; tl < tiles && ok; tl += tstep) {
 #pragma unroll
         for (int i = 0; i < 2 * NA; ++i) v[i] = __float_as_uint(__uint_as_float(v[i]) * kScale);
         for (int b = 0; b < nb; ++b) {
             const SetSlots &ss = sset[b];
             unsigned slot = (unsigned)ss.lo[r & 31u] ^ (unsigned)ss.hi[r >> 5];
             if (H == 2 && hh) slot ^= ss.q[4];
+            if (PH && d.op_kind[b] == 1) {
+                // Phase op: each amplitude times its table entry, in place
+                // (the layout stays).  Every thread waits for the operands
+                // itself (bounded; a wait that gives up is reported).
+                if (!t_ready) {
+                    t_ready = mbar_wait(bb, 0u);
+                    if (!t_ready) atomicOr(&g_tc_status, 1u);
+                }
+                const float2 *tab = (const float2 *)(Bs + d.op_off[b]);
+#pragma unroll
+                for (int i = 0; i < NA; ++i) {
+                    const int j = i ^ (i >> 1);
+                    if (i > 0) slot ^= ss.q[gray_bit(i)];
+                    const float2 p = tab[slot];
+                    const float x = __uint_as_float(v[2 * j]), y = __uint_as_float(v[2 * j + 1]);
+                    v[2 * j] = __float_as_uint(fmaf(x, p.x, -y * p.y));
+                    v[2 * j + 1] = __float_as_uint(fmaf(x, p.y, y * p.x));
+                }
+                continue;
+            }
             unsigned q[NB];
 #pragma unroll
             for (int k = 0; k < NB; ++k) q[k] = ss.q[k];
@@ -314,7 +320,7 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
                 if (b_ready) {
                     tc_fence_after();
                     const unsigned ah = smem_u32(Ah), al = smem_u32(Al),
-                                   bh = smem_u32(Bs + (size_t)b * kBBytes), bl = bh + kBBytes / 2;
+                                   bh = smem_u32(Bs + d.op_off[b]), bl = bh + kBBytes / 2;
                     // The tensor core rounds its FP32 accumulator toward zero
                     // at every MMA, which shrinks magnitudes: the correction
                     // products go first (small values), the main product's
@@ -392,10 +398,14 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
         group_sync(gbar, TG);
         if (tl + tstep < tiles) load_raw(tl + tstep);
         {
-            unsigned slot = pt;
+            // the natural tile read in the load layout
+            const SetSlots &nat = sset[nb + 1];
+            unsigned slot = (unsigned)nat.lo[r & 31u] ^ (unsigned)nat.hi[r >> 5];
+            if (H == 2 && hh) slot ^= nat.q[4];
+            float2 *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | row_offset());
             gray_walk<NB>(gp, e, [&](int j, float2 *p) {
                 const int i = gray_index(j);
-                if (i > 0) slot ^= qn[gray_bit(i)];
+                if (i > 0) slot ^= nat.q[gray_bit(i)];
                 *p = tile_sm[slot];
             });
         }
@@ -415,44 +425,61 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, long lon
 }
 
 // Shared memory of the persistent kernel: G tiles' operand pairs, the
-// stage's block operands and the slot tables.
-static size_t tstage_smem(int m, int groups, int nblocks) {
-    return (size_t)groups * 2 * ((size_t)4 << m) + (size_t)nblocks * 2 * 64 * 64 * 2 +
-           sizeof(SetSlots) * (size_t)(nblocks + 2);
+// stage's op operands and the slot tables.
+static size_t tstage_smem(int m, int groups, size_t ops_bytes, int nops) {
+    return (size_t)groups * 2 * ((size_t)4 << m) + ops_bytes +
+           sizeof(SetSlots) * (size_t)(nops + 2);
 }
 
 // Groups per CTA: 4 for 12-lane tiles (of 128 threads, or of 256 with two
 // threads per row), 2 of 256 threads for 13-lane tiles.
 static int tstage_groups(int m) { return m == 12 ? 4 : 2; }
 
-int tstage_max_blocks(int m) {
-    const int groups = tstage_groups(m);
-    int nb = 1;
-    while (nb < kMaxTcBlocks && tstage_smem(m, groups, nb + 1) + 2048 <= 227 * 1024) ++nb;
-    return nb;
-}
-
 void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool two_per_row) {
     if (d.m != 12 && d.m != 13) fail(2, "tensor stage: tile lanes must be 12 or 13 (got %d)", d.m);
-    if (d.nblocks < 1 || d.nblocks > tstage_max_blocks(d.m))
-        fail(2, "tensor stage: bad block count %d", d.nblocks);
-    if (((uintptr_t)d.bmats & 15u) != 0) fail(2, "tensor stage: operand array misaligned");
-    const long long tiles = 1LL << (d.n - d.m);
+    if (d.nblocks < 1 || d.nblocks > kMaxTcBlocks) fail(2, "tensor stage: bad op count %d", d.nblocks);
+    if (((uintptr_t)d.bmats & 15u) != 0 || (d.ops_bytes & 15u) != 0)
+        fail(2, "tensor stage: operand array misaligned");
+    // Every slot a thread forms (an XOR of table entries) is at most the OR
+    // of the table's entries: it must stay inside the tile operand (dense
+    // ops), the op's table (phase ops) or the natural tile.
+    auto reach = [](const SetSlots &ss) {
+        unsigned any = 0;
+        for (unsigned short x : ss.lo) any |= x;
+        for (unsigned short x : ss.hi) any |= x;
+        for (unsigned short x : ss.q) any |= x;
+        return any;
+    };
+    for (int b = 0; b < d.nblocks + 2; ++b) {
+        const unsigned any = reach(d.sets[b]);
+        const bool phase = b < d.nblocks && d.op_kind[b] == 1;
+        if (!phase && any >= (1u << d.m)) fail(2, "tensor stage: slot table %d outside the tile", b);
+        if (b >= d.nblocks) continue;
+        const unsigned need = phase ? 8u * (any + 1u) : 2u * 64u * 64u * 2u;
+        if ((d.op_off[b] & 15u) != 0 || d.op_off[b] + need > d.ops_bytes)
+            fail(2, "tensor stage: op %d operands outside the operand array", b);
+    }
+    if (tstage_smem(d.m, tstage_groups(d.m), d.ops_bytes, d.nblocks) + 2048 > 227 * 1024)
+        fail(2, "tensor stage: %u bytes of operands do not fit in shared memory", d.ops_bytes);
+    if (d.n - d.m > 30) fail(2, "tensor stage: %d lanes are too many", d.n);
+    const int tiles = 1 << (d.n - d.m);
     int dev = 0, sms = 0;
     QG_CUDA(cudaGetDevice(&dev));
     QG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     auto launch = [&](auto kern, int groups, int threads) {
-        const size_t smem = tstage_smem(d.m, groups, d.nblocks);
+        const size_t smem = tstage_smem(d.m, groups, d.ops_bytes, d.nblocks);
         QG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        const long long ctas = std::min<long long>((tiles + groups - 1) / groups, sms);
+        const int ctas = std::min((tiles + groups - 1) / groups, sms);
         kern<<<(unsigned)ctas, threads, smem, stream>>>((float2 *)state, d, tiles);
     };
+    bool phases = false;
+    for (int b = 0; b < d.nblocks; ++b) phases = phases || d.op_kind[b] == 1;
     if (d.m == 12 && two_per_row)
-        launch(k_tstage<1, 3, 2>, 3, 768);
+        phases ? launch(k_tstage<1, 3, 2, true>, 3, 768) : launch(k_tstage<1, 3, 2, false>, 3, 768);
     else if (d.m == 12)
-        launch(k_tstage<1, 4, 1>, 4, 512);
+        phases ? launch(k_tstage<1, 4, 1, true>, 4, 512) : launch(k_tstage<1, 4, 1, false>, 4, 512);
     else
-        launch(k_tstage<2, 2, 1>, 2, 512);
+        phases ? launch(k_tstage<2, 2, 1, true>, 2, 512) : launch(k_tstage<2, 2, 1, false>, 2, 512);
     QG_CUDA(cudaGetLastError());
 }
 

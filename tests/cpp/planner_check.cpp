@@ -7,6 +7,7 @@
 
 #include <cstdio>
 #include <random>
+#include <map>
 #include <set>
 
 using namespace qg;
@@ -22,7 +23,8 @@ static PendingGate make_gate(int t, std::vector<int> c, cd a, cd b, cd cc, cd d)
     return g;
 }
 
-static std::vector<PendingGate> random_gates(std::mt19937 &rng, int n, int count) {
+static std::vector<PendingGate> random_gates(std::mt19937 &rng, int n, int count,
+                                             int dense_in_4 = 3) {
     std::uniform_real_distribution<double> U(0, 6.283185307179586);
     std::vector<PendingGate> out;
     for (int i = 0; i < count; ++i) {
@@ -34,7 +36,7 @@ static std::vector<PendingGate> random_gates(std::mt19937 &rng, int n, int count
             if (x != t && std::find(c.begin(), c.end(), x) == c.end()) c.push_back(x);
         }
         const double th = U(rng), ph = U(rng), la = U(rng);
-        if (rng() % 4 == 0)  // diagonal
+        if ((int)(rng() % 4) >= dense_in_4)  // diagonal
             out.push_back(make_gate(t, c, 1., 0., 0., std::polar(1., ph)));
         else
             out.push_back(make_gate(t, c, std::cos(th / 2), -std::polar(std::sin(th / 2), la),
@@ -182,39 +184,138 @@ int main(int argc, char **argv) {
             for (unsigned ti = 0; ti < 4096; ++ti) seen.insert(tc_operand_slot(L, ti));
             if (seen.size() != 4096 || *seen.rbegin() >= 4096) ++bad_slots;
         }
-        int bad_tables = 0, launches = 0;
-        for (int trial = 0; trial < 10; ++trial) {
+        int bad_tables = 0, launches = 0, phase_ops = 0, dense_ops = 0;
+        double worst_emul = 0.;
+        auto b_index = [](int k, int nn) {  // the FP16 index of B[k][n] in Bh (Bl: + 4096)
+            return (size_t)(k / 16) * 1024 + (k % 16 / 8) * 512 + (nn / 8) * 64 + (nn % 8) * 8 + k % 8;
+        };
+        for (int trial = 0; trial < 24; ++trial) {
+            const int m = trial % 3 == 2 ? 13 : 12, t = m - 5, TR = 1 << t;
             const int n = 20;
-            auto gates = random_gates(rng, n, 120);
+            auto gates = random_gates(rng, n, 160, trial % 2 ? 1 : 3);  // odd: mostly diagonal
             std::vector<const PendingGate *> rem;
             for (auto &g : gates) rem.push_back(&g);
             const unsigned long long base = 15;
-            const unsigned long long S0 = plan_stage_lanes(rem, base, 12);
+            const unsigned long long S0 = plan_stage_lanes(rem, base, m);
             std::vector<const PendingGate *> take, keep;
             stage_take(rem, S0, rem.size(), &take, &keep);
             if (take.size() < 2) continue;
             unsigned long long SS = S0;
-            for (int q = 0; q < n && __builtin_popcountll(SS) < 12; ++q) SS |= 1ULL << q;
+            for (int q = 0; q < n && __builtin_popcountll(SS) < m; ++q) SS |= 1ULL << q;
             TileLanes tl = tile_lanes_of(SS, n);
-            auto blocks = tc_blocks(take, tl);
-            const int nb = (int)std::min<size_t>(6, blocks.size());
+            const TcOps ops = tc_ops(tc_blocks(take, tl), true);
+            const int nb = tc_ops_per_launch(ops, 0);
             static TcStageDesc desc;
-            static unsigned short ops[6 * 2 * 64 * 64];
-            tc_plan_launch(tl, n, blocks, 0, nb, desc, ops);
+            static unsigned char buf[128 * 1024];
+            tc_plan_launch(tl, n, ops, 0, nb, desc, buf);
             ++launches;
-            for (int b = 0; b <= nb + 1; ++b) {  // every set: 128 rows x 32 registers -> 4096 slots
-                const SetSlots &ss = desc.sets[b];
-                std::set<unsigned> seen;
-                for (unsigned r = 0; r < 128; ++r)
-                    for (unsigned j = 0; j < 32; ++j) {
-                        unsigned slot = (unsigned)ss.lo[r & 31u] ^ (unsigned)ss.hi[r >> 5];
-                        for (int k = 0; k < 5; ++k)
-                            if (j >> k & 1u) slot ^= ss.q[k];
-                        seen.insert(slot);
-                    }
-                if (seen.size() != 4096) ++bad_tables;
+            auto slot_of = [&](const SetSlots &ss, unsigned r, unsigned j) {
+                unsigned slot = (unsigned)ss.lo[r & 31u] ^ (unsigned)ss.hi[r >> 5];
+                for (int k = 0; k < 5; ++k)
+                    if (j >> k & 1u) slot ^= ss.q[k];
+                return slot;
+            };
+            // dense ops and the natural tile: TR rows x 32 registers onto the
+            // tile's slots once; phase ops: onto the table entries equally often
+            for (int b = 0; b < nb + 2; ++b) {
+                const bool phase = b < nb && desc.op_kind[b] == 1;
+                if (b < nb) {
+                    (phase ? phase_ops : dense_ops) += 1;
+                    if (desc.op_off[b] % 16 || desc.op_off[b] + tc_op_bytes(ops[b]) > desc.ops_bytes)
+                        ++bad_tables;
+                }
+                std::map<unsigned, int> seen;
+                for (unsigned r = 0; r < (unsigned)TR; ++r)
+                    for (unsigned j = 0; j < 32; ++j) seen[slot_of(desc.sets[b], r, j)] += 1;
+                const size_t entries = phase ? tc_op_bytes(ops[b]) / 8 : (size_t)1 << m;
+                if (seen.size() != entries || seen.rbegin()->first >= entries) ++bad_tables;
+                for (auto &kv : seen)
+                    if (kv.second != (int)(((size_t)1 << m) / entries)) ++bad_tables;
             }
+            // Emulation of the kernel's data flow in FP64 on a random tile:
+            // load layout -> per op (dense: scatter through the slot table,
+            // D = A (Bh + Bl) from the operand buffer, rows back in the new
+            // layout; phase: times the table entry) -> natural tile ->
+            // load layout; against the ops' gates applied to the tile directly.
+            std::map<long long, cd> want;
+            std::normal_distribution<double> gauss(0, 1);
+            auto load_off = [&](unsigned r, unsigned j) {
+                long long lo = desc.dep_hi[j];
+                for (int b = 0; b < t; ++b)
+                    if (r >> b & 1u) lo |= 1LL << desc.row_lane[b];
+                return lo;
+            };
+            std::vector<std::vector<cd>> V(TR, std::vector<cd>(32));
+            for (unsigned r = 0; r < (unsigned)TR; ++r)
+                for (unsigned j = 0; j < 32; ++j)
+                    want[load_off(r, j)] = V[r][j] = cd(gauss(rng), gauss(rng));
+            if (want.size() != ((size_t)1 << m)) ++bad_tables;
+            for (int b = 0; b < nb; ++b) {
+                const SetSlots &ss = desc.sets[b];
+                if (desc.op_kind[b] == 1) {
+                    const float *tab = (const float *)(buf + desc.op_off[b]);
+                    for (unsigned r = 0; r < (unsigned)TR; ++r)
+                        for (unsigned j = 0; j < 32; ++j) {
+                            const unsigned e = slot_of(ss, r, j);
+                            V[r][j] *= cd(tab[2 * e], tab[2 * e + 1]);
+                        }
+                    continue;
+                }
+                std::vector<cd> A((size_t)1 << m);
+                for (unsigned r = 0; r < (unsigned)TR; ++r)
+                    for (unsigned j = 0; j < 32; ++j) A[slot_of(ss, r, j)] = V[r][j];
+                const unsigned short *B = (const unsigned short *)(buf + desc.op_off[b]);
+                for (unsigned row = 0; row < (unsigned)TR; ++row) {
+                    // unswizzled slot (row << 5) | i holds amplitude i of the
+                    // operand row; the 128-byte swizzle XORs bits 2..4 with 5..7
+                    double arow[64];
+                    for (unsigned i = 0; i < 32; ++i) {
+                        const unsigned c = (row << 5) | i;
+                        const unsigned cs = c ^ (((c >> 5) & 7u) << 2);
+                        arow[2 * i] = A[cs].real();
+                        arow[2 * i + 1] = A[cs].imag();
+                    }
+                    for (int o = 0; o < 32; ++o) {
+                        double re = 0, im = 0;
+                        for (int k = 0; k < 64; ++k) {
+                            const size_t i0 = b_index(k, 2 * o), i1 = b_index(k, 2 * o + 1);
+                            re += arow[k] * (f16_value(B[i0]) + f16_value(B[4096 + i0]));
+                            im += arow[k] * (f16_value(B[i1]) + f16_value(B[4096 + i1]));
+                        }
+                        V[row][o] = cd(re, im);
+                    }
+                }
+            }
+            // copy-out: final layout -> natural tile -> load layout
+            std::vector<cd> nat((size_t)1 << m);
+            for (unsigned r = 0; r < (unsigned)TR; ++r)
+                for (unsigned j = 0; j < 32; ++j) nat[slot_of(desc.sets[nb], r, j)] = V[r][j];
+            std::map<long long, cd> got;
+            for (unsigned r = 0; r < (unsigned)TR; ++r)
+                for (unsigned j = 0; j < 32; ++j)
+                    got[load_off(r, j)] = nat[slot_of(desc.sets[nb + 1], r, j)];
+            for (int b = 0; b < nb; ++b)
+                for (auto *g : ops[b].gates) {
+                    const long long tb = 1LL << g->target;
+                    long long cm = 0;
+                    for (int c : g->controls) cm |= 1LL << c;
+                    const cd m00(g->m.v[0], g->m.v[1]), m01(g->m.v[2], g->m.v[3]),
+                        m10(g->m.v[4], g->m.v[5]), m11(g->m.v[6], g->m.v[7]);
+                    for (auto &kv : want) {
+                        const long long off = kv.first;
+                        if ((off & tb) || (off & cm) != cm) continue;
+                        const cd a0 = want[off], a1 = want[off | tb];
+                        want[off] = m00 * a0 + m01 * a1;
+                        want[off | tb] = m10 * a0 + m11 * a1;
+                    }
+                }
+            double nrm = 0;
+            for (auto &kv : want) nrm = std::max(nrm, std::abs(kv.second));
+            for (auto &kv : want)
+                worst_emul = std::max(worst_emul, std::abs(got[kv.first] - kv.second) / nrm);
         }
+        printf("emulated_stage_max_rel_err %.3e\nphase_ops %d\ndense_ops %d\n", worst_emul,
+               phase_ops, dense_ops);
         printf("bad_slots %d\nbad_tables %d\nlaunches_checked %d\n", bad_slots, bad_tables, launches);
     }
     return 0;
