@@ -401,7 +401,7 @@ def run_gb300(args):
         adjoint = run_adjoint(args)
 
     c4 = None
-    if rank == 0 and args.c4:
+    if rank == 0 and not args.no_c4:
         qs.delete()
         nat.call('qg_devices_clear')
         c4 = run_c4(args, rt, nat)
@@ -532,8 +532,11 @@ def qft_ops(n, seed):
 
 def run_compiled(args, rt, nat):
     """Per-run latency of whole circuits through the plugin API with one call
-    per gate (the reference front-end's pattern), against `CompiledCircuit`
-    (the gate table in one call) and its CUDA-graph replay: the reference's
+    per gate (the reference front-end's pattern; with trace replay, the
+    default, a run seen before replays its captured CUDA graph, and without
+    it, `per_gate_call_planned_ms`, every run is planned anew), against
+    `CompiledCircuit` (the gate table in one call) and its CUDA-graph replay:
+    the reference's
     20-qubit QFT case (complex128, and complex64, where the device work is
     small and the host's share shows; X preparation from default_rng(0)) and
     the headline random circuit (complex64).  Wall time from reset to a
@@ -570,8 +573,15 @@ def run_compiled(args, rt, nat):
                 ts.append(time.perf_counter() - t0)
             return float(np.median(ts)) * 1e3
 
+        nat.set_trace_replay(False)
+        planned = median_ms(per_gate)
+        nat.set_trace_replay(True)
+        nat.trace_stats(reset=True)
+        replayed = median_ms(per_gate)
+        st = nat.trace_stats(reset=True)
         res = {'qubits': n, 'gates': len(gts), 'dtype': 'c128' if dtype == np.float64 else 'c64',
-               'per_gate_call_ms': median_ms(per_gate)}
+               'per_gate_call_ms': replayed, 'per_gate_call_planned_ms': planned,
+               'trace_replays': st['hits'], 'trace_captures': st['captures']}
         for graph in (False, True):
             circ = CompiledCircuit(dtype, gts, graph=graph)
 
@@ -600,6 +610,8 @@ def run_c4(args, rt, nat):
     from qgate_gb300 import autotune
     out = {}
 
+    peak, peak_kind = measured_peak_hbm()
+
     def run(n, ops, label):
         gts = [(gate_type(nm, *a), t, list(c)) for nm, a, t, c in ops]
         qs = rt.create_qubit_states(np.float32)
@@ -608,6 +620,8 @@ def run_c4(args, rt, nat):
         proc.reset_qubit_states(qs)
         proc.synchronize()
         nat.gate_stats(reset=True)
+        nat.timing_all(reset=True)
+        nat.timing_enable(True)
         t0 = time.perf_counter()
         for gt, t, c in gts:
             if c:
@@ -616,11 +630,20 @@ def run_c4(args, rt, nat):
                 proc.apply_gate(gt, False, qs, t)
         proc.synchronize()
         dt = time.perf_counter() - t0
+        nat.timing_enable(False)
+        tm = nat.timing_all(reset=True)
         st = nat.gate_stats(reset=True)
-        out[label] = {'qubits': n, 'gates': len(ops), 'passes': st['passes'], 'ms': dt * 1e3,
-                      'gate_pass_gbs': gate_pass_bytes(n, ops, 8) / dt / 1e9,
-                      'hbm_gbs_actual': st['bytes'] / dt / 1e9,
-                      'norm': qs.processor.calc_norm(qs)}
+        res = {'qubits': n, 'gates': len(ops), 'passes': st['passes'], 'ms': dt * 1e3,
+               'gate_pass_gbs': gate_pass_bytes(n, ops, 8) / dt / 1e9,
+               'hbm_gbs_actual': st['bytes'] / dt / 1e9,
+               'kernel_ms': {k: v[1] for k, v in tm.items() if v[0]},
+               'norm': qs.processor.calc_norm(qs)}
+        launches, ms = tm.get('tstage', (0, 0.))
+        if launches:
+            gbs = 2 * (1 << n) * 8 / (ms / launches / 1e3) / 1e9
+            res['tstage'] = {'launches': launches, 'avg_launch_ms': ms / launches, 'gbs': gbs,
+                             'frac_of_peak': gbs / peak, 'peak_source': peak_kind}
+        out[label] = res
         return qs
 
     n1 = args.c4_random_qubits
@@ -634,7 +657,7 @@ def run_c4(args, rt, nat):
 
     n2 = args.c4_qft_qubits
     qs = run(n2, qft_ops(n2, 41), 'qft_%dq' % n2)
-    pr = [qs.processor.calc_probability(qs, q) for q in range(0, n2, 5)]
+    pr = [qs.processor.calc_probability(qs, q) for q in range(n2)]
     out['qft_%dq' % n2]['max_abs_pr0_minus_half'] = float(max(abs(p - 0.5) for p in pr))
     getter = rt.create_qubits_states_getter(np.float32)
     t0 = time.perf_counter()
@@ -818,7 +841,7 @@ def main():
     ap.add_argument('--no-adjoint', action='store_true')
     ap.add_argument('--no-batch', action='store_true')
     ap.add_argument('--no-compiled', action='store_true')
-    ap.add_argument('--c4', action='store_true', help='also run the 33/34-qubit large states')
+    ap.add_argument('--no-c4', action='store_true', help='skip the 33/34-qubit large states')
     ap.add_argument('--c4-random-qubits', type=int, default=33)
     ap.add_argument('--c4-qft-qubits', type=int, default=34)
     ap.add_argument('--c4-samples', type=int, default=100_000_000)

@@ -142,6 +142,21 @@ int qg_circuit_run(qg_handle circuit, qg_handle qstates);
 int qg_circuit_stats(qg_handle circuit, int *captured, int64_t *passes);
 int qg_circuit_delete(qg_handle circuit);
 
+/* Extension: trace replay for the per-gate path.  The reference front-end
+ * applies a circuit one apply_gate / apply_controlled_gate call at a time
+ * (qgate/simulator/rop_executor.py:28-34) and every run is planned anew.  With
+ * trace replay on (default), a run of queued gates flushed at an observation
+ * is remembered (the last 8 distinct runs of >= 8 gates); when the same run
+ * (same gates, lanes, matrices, precision and lane count) is flushed again,
+ * the second time its stages are captured into a CUDA graph and from then on
+ * the graph is replayed with no host planning, giving the same state as
+ * planning would.  Runs partly launched while still being enqueued (>= 640
+ * pending gates) are planned as usual.  qg_set_trace_replay(0) turns it off
+ * and frees the remembered runs; qg_trace_stats reports graph replays and
+ * captures (reset: clear the counters). */
+int qg_set_trace_replay(int on);
+int qg_trace_stats(int64_t *hits, int64_t *captures, int reset);
+
 /* Extension: dense 2^k x 2^k complex128 matrix (row-major, interleaved re/im)
  * on k target lanes (targets[0] = least significant matrix bit), optionally
  * controlled.  k <= 6.  Replaces the reference's expansions of multi-qubit

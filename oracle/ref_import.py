@@ -19,9 +19,19 @@ import types
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
+# Where the reference's sources are mounted in the build container; the
+# QGATE_REF_ROOT environment variable overrides it.  Only the scripts that
+# read the reference itself (the fixture generators, the oracle's reference
+# build) use it.
+DEFAULT_REF_ROOT = '/root/reference'
+
+
+def reference_root():
+    return os.environ.get('QGATE_REF_ROOT', DEFAULT_REF_ROOT)
+
 
 def import_reference(ref_root=None):
-    ref_root = ref_root or os.environ.get('QGATE_REF_ROOT', '/root/reference')
+    ref_root = ref_root or reference_root()
     if 'qgate' in sys.modules and hasattr(sys.modules['qgate'], 'simulator'):
         return sys.modules['qgate']
     if not os.path.isdir(os.path.join(ref_root, 'qgate')):

@@ -9,8 +9,10 @@ Every function restates the algorithm of the reference file:line it names
 (qgate 0.2.2).  States are complex128 (the reference's FP64 oracle runtime)
 unless a complex64 array is passed in.  Index bit i of an amplitude is local
 lane i.  The restatement is pinned against golden vectors produced by running
-the reference itself (`tests/golden/make_golden.py`) and against the
-reference's own known-answer tests (`tests/test_oracle_golden.py`).
+the reference itself (`tests/golden/make_golden.py`, replayed by
+`tests/test_oracle_replay.py`), the matrices recorded from it
+(`tests/test_cpu_abi.py`) and its parameter-shift gradients
+(`tests/test_oracle_adjoint.py`).
 """
 import cmath
 import math

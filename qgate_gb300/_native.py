@@ -61,6 +61,8 @@ SIGNATURES = {
     'qg_set_fusion': [_i],
     'qg_set_fusion_params': [_i, _i, _i, _i],
     'qg_set_stage_pipelining': [_i],
+    'qg_set_trace_replay': [_i],
+    'qg_trace_stats': [_i64p, _i64p, _i],
     'qg_set_tensor_blocks': [_i],
     'qg_tensor_stage_status': [_i, _ip],
     'qg_set_host_direct': [_i],
@@ -164,8 +166,20 @@ def set_fusion_params(prec, tile_lanes, reg_lanes, cost_budget=0):
 
 def set_tensor_blocks(on):
     """Run complex64 stages of 12/13-lane tiles as fused 5-lane blocks on the
-    tensor cores (tcgen05, 3xTF32)."""
+    tensor cores (tcgen05 kind::f16 on split FP16 operands)."""
     call('qg_set_tensor_blocks', 1 if on else 0)
+
+
+def set_trace_replay(on):
+    """Replay recurring runs of per-gate calls from captured CUDA graphs."""
+    call('qg_set_trace_replay', 1 if on else 0)
+
+
+def trace_stats(reset=False):
+    """{'hits': graph replays, 'captures': runs captured} of trace replay."""
+    h, c = _i64(0), _i64(0)
+    check(lib.qg_trace_stats(ctypes.byref(h), ctypes.byref(c), 1 if reset else 0))
+    return {'hits': h.value, 'captures': c.value}
 
 
 def tensor_stage_status(reset=False):

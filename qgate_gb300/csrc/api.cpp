@@ -117,6 +117,7 @@ struct States {
     int n_lanes = -1;
     void *d = nullptr;
     std::vector<PendingGate> pending;
+    bool streamed = false;  // part of the pending run was launched by the streaming flush
 };
 
 struct Processor {
@@ -212,6 +213,17 @@ struct Device {
     std::unordered_set<Getter *> getters;
     std::unordered_set<Pool *> pools;
     std::unordered_set<struct Circuit *> circuits;
+    // Trace replay: gate runs that recur between observations (the same
+    // gates on the same lanes, e.g. a circuit run again through the plugin
+    // API) are kept as circuits and replayed from a captured CUDA graph.
+    bool trace_replay = true;
+    struct Trace {
+        unsigned long long hash = 0;
+        long long used = 0;
+        struct Circuit *c = nullptr;
+    };
+    std::vector<Trace> traces;
+    long long trace_clock = 0, trace_hits = 0, trace_captures = 0;
     std::recursive_mutex mu;
 };
 
@@ -720,6 +732,7 @@ static void stream_flush(States *s) {
     merge_runs(s->pending);
     std::vector<const PendingGate *> remaining;
     for (auto &g : s->pending) remaining.push_back(&g);
+    s->streamed = true;
     flush_lookahead(d, s, remaining, base, M, 1);
     std::vector<PendingGate> rest;
     rest.reserve(remaining.size());
@@ -734,9 +747,16 @@ static void stream_flush(States *s) {
 // lane sets are disjoint).  The lowest lanes are always in S so that each
 // tile is made of >= 128-byte contiguous runs.  A per-amplitude cost budget
 // closes a stage before its arithmetic outgrows its HBM time.
+static bool replay_trace(Device &d, States *s);
+
 static void flush(States *s) {
-    if (s->pending.empty()) return;
+    if (s->pending.empty()) {
+        s->streamed = false;
+        return;
+    }
     Device &d = dev();
+    if (replay_trace(d, s)) return;
+    s->streamed = false;
     const int n = s->n_lanes;
     int M = d.tile_lanes[s->prec];
     if (M <= 1) {
@@ -1020,6 +1040,164 @@ static void adjoint2(double *m) {
     m[7] = -t[7];
 }
 
+// ------------------------------------------------------------ compiled circuits
+
+static void drop_graph(Device &d, Circuit *c) {
+    if (c->exec || !c->chunks.empty()) QG_CUDA(cudaStreamSynchronize(d.stream));
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    if (c->g) cudaGraphDestroy(c->g);
+    for (auto &ch : c->chunks) {
+        cudaFreeHost(ch.first);
+        cudaFree(ch.second);
+    }
+    c->chunks.clear();
+    c->chunk_off = 0;
+    c->exec = nullptr;
+    c->g = nullptr;
+    c->state = nullptr;
+    c->n_lanes = -1;
+}
+
+// Plans the circuit's gates on s under stream capture (nothing runs) and
+// instantiates the graph.  The states object's queue must be empty.
+static void capture_circuit(Device &d, Circuit *c, States *s) {
+    const bool timing = d.timing;
+    const long long p0 = d.n_passes, b0 = d.n_bytes;
+    d.timing = false;
+    d.capturing = c;
+    cudaGraph_t graph = nullptr;
+    auto restore = [&] {
+        d.capturing = nullptr;
+        d.timing = timing;
+        d.n_passes = p0;
+        d.n_bytes = b0;
+        s->pending.clear();
+    };
+    QG_CUDA(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeRelaxed));
+    try {
+        s->pending = c->gates;
+        flush(s);
+    } catch (...) {
+        cudaStreamEndCapture(d.stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        restore();
+        throw;
+    }
+    const cudaError_t ec = cudaStreamEndCapture(d.stream, &graph);
+    c->passes = d.n_passes - p0;
+    c->bytes = d.n_bytes - b0;
+    restore();
+    cuda_check(ec, "cudaStreamEndCapture");
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    if (ei != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        cuda_check(ei, "cudaGraphInstantiate");
+    }
+    c->g = graph;
+    c->exec = exec;
+    c->state = s->d;
+    c->n_lanes = s->n_lanes;
+    c->version = d.settings_version;
+}
+
+// ------------------------------------------------------------ trace replay
+
+constexpr size_t kTraceMinGates = 8, kTraceSlots = 8;
+
+static unsigned long long trace_hash(const States *s, const std::vector<PendingGate> &gates) {
+    unsigned long long h = 1469598103934665603ULL;  // FNV-1a
+    auto mix = [&](const void *p, size_t n) {
+        const unsigned char *b = (const unsigned char *)p;
+        for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ULL;
+    };
+    mix(&s->prec, sizeof(s->prec));
+    mix(&s->n_lanes, sizeof(s->n_lanes));
+    for (const auto &g : gates) {
+        mix(&g.target, sizeof(g.target));
+        const int nc = (int)g.controls.size();
+        mix(&nc, sizeof(nc));
+        if (nc) mix(g.controls.data(), sizeof(int) * (size_t)nc);
+        mix(g.m.v, sizeof(g.m.v));
+    }
+    return h;
+}
+
+static bool same_gates(const std::vector<PendingGate> &a, const std::vector<PendingGate> &b) {
+    if (a.size() != b.size()) return false;
+    for (size_t i = 0; i < a.size(); ++i)
+        if (a[i].target != b[i].target || a[i].controls != b[i].controls ||
+            memcmp(a[i].m.v, b[i].m.v, sizeof(a[i].m.v)) != 0)
+            return false;
+    return true;
+}
+
+// Called by flush() with the states object's pending gates (a whole run
+// since the last flush, none of it launched yet).  A run seen before is
+// applied from its circuit: the second time it is planned under stream
+// capture into a CUDA graph, every later time the graph is replayed with no
+// host planning; the plan is the same, so the state is the same.  A new run
+// is remembered (the least recently used of kTraceSlots is forgotten) and
+// planned as usual.  Returns whether the run was applied here.
+static bool replay_trace(Device &d, States *s) {
+    if (!d.trace_replay || d.capturing || s->streamed || s->pending.size() < kTraceMinGates)
+        return false;
+    const unsigned long long h = trace_hash(s, s->pending);
+    Device::Trace *hit = nullptr;
+    for (auto &t : d.traces)
+        if (t.hash == h && t.c->prec == s->prec && same_gates(t.c->gates, s->pending)) {
+            hit = &t;
+            break;
+        }
+    if (!hit) {
+        Circuit *c = new Circuit();
+        c->prec = s->prec;
+        c->graph = true;
+        c->gates = s->pending;
+        Device::Trace t;
+        t.hash = h;
+        t.c = c;
+        t.used = ++d.trace_clock;
+        if (d.traces.size() < kTraceSlots) {
+            d.traces.push_back(t);
+        } else {
+            auto lru = std::min_element(d.traces.begin(), d.traces.end(),
+                                        [](const Device::Trace &a, const Device::Trace &b) {
+                                            return a.used < b.used;
+                                        });
+            if (lru->c->exec || !lru->c->chunks.empty()) drop_graph(d, lru->c);
+            delete lru->c;
+            *lru = t;
+        }
+        return false;  // planned as usual
+    }
+    hit->used = ++d.trace_clock;
+    Circuit *c = hit->c;
+    std::vector<PendingGate> run;
+    run.swap(s->pending);  // capture_circuit wants the queue empty
+    if (c->exec && (c->state != s->d || c->n_lanes != s->n_lanes ||
+                    c->version != d.settings_version))
+        drop_graph(d, c);
+    if (!c->exec) {
+        capture_circuit(d, c, s);
+        d.trace_captures += 1;
+    } else {
+        d.trace_hits += 1;
+    }
+    QG_CUDA(cudaGraphLaunch(c->exec, d.stream));
+    d.n_passes += c->passes;
+    d.n_bytes += c->bytes;
+    return true;
+}
+
+static void drop_traces(Device &d) {
+    for (auto &t : d.traces) {
+        if (t.c->exec || !t.c->chunks.empty()) drop_graph(d, t.c);
+        delete t.c;
+    }
+    d.traces.clear();
+}
+
 }  // namespace qg
 
 using namespace qg;
@@ -1069,6 +1247,7 @@ int qg_devices_clear(void) {
     if (g_dev.initialized) {
         QG_CUDA(cudaSetDevice(g_dev.dev));
         cudaStreamSynchronize(g_dev.stream);
+        drop_traces(g_dev);
         g_dev.arena.trim();
     }
     QG_END
@@ -1316,63 +1495,20 @@ int qg_qubit_processor_apply_controlled_gate(qg_handle hp, const double *mat, qg
 
 // ------------------------------------------------------------ compiled circuits
 
-static void drop_graph(Device &d, Circuit *c) {
-    if (c->exec || !c->chunks.empty()) QG_CUDA(cudaStreamSynchronize(d.stream));
-    if (c->exec) cudaGraphExecDestroy(c->exec);
-    if (c->g) cudaGraphDestroy(c->g);
-    for (auto &ch : c->chunks) {
-        cudaFreeHost(ch.first);
-        cudaFree(ch.second);
-    }
-    c->chunks.clear();
-    c->chunk_off = 0;
-    c->exec = nullptr;
-    c->g = nullptr;
-    c->state = nullptr;
-    c->n_lanes = -1;
+int qg_set_trace_replay(int on) {
+    QG_BEGIN
+    flush_all();
+    g_dev.trace_replay = on != 0;
+    if (!on) drop_traces(g_dev);
+    QG_END
 }
 
-// Plans the circuit's gates on s under stream capture (nothing runs) and
-// instantiates the graph.  The states object's queue must be empty.
-static void capture_circuit(Device &d, Circuit *c, States *s) {
-    const bool timing = d.timing;
-    const long long p0 = d.n_passes, b0 = d.n_bytes;
-    d.timing = false;
-    d.capturing = c;
-    cudaGraph_t graph = nullptr;
-    auto restore = [&] {
-        d.capturing = nullptr;
-        d.timing = timing;
-        d.n_passes = p0;
-        d.n_bytes = b0;
-        s->pending.clear();
-    };
-    QG_CUDA(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeRelaxed));
-    try {
-        s->pending = c->gates;
-        flush(s);
-    } catch (...) {
-        cudaStreamEndCapture(d.stream, &graph);
-        if (graph) cudaGraphDestroy(graph);
-        restore();
-        throw;
-    }
-    const cudaError_t ec = cudaStreamEndCapture(d.stream, &graph);
-    c->passes = d.n_passes - p0;
-    c->bytes = d.n_bytes - b0;
-    restore();
-    cuda_check(ec, "cudaStreamEndCapture");
-    cudaGraphExec_t exec = nullptr;
-    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
-    if (ei != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        cuda_check(ei, "cudaGraphInstantiate");
-    }
-    c->g = graph;
-    c->exec = exec;
-    c->state = s->d;
-    c->n_lanes = s->n_lanes;
-    c->version = d.settings_version;
+int qg_trace_stats(int64_t *hits, int64_t *captures, int reset) {
+    QG_BEGIN
+    *hits = g_dev.trace_hits;
+    *captures = g_dev.trace_captures;
+    if (reset) g_dev.trace_hits = g_dev.trace_captures = 0;
+    QG_END
 }
 
 int qg_circuit_new(int prec, int n_gates, const int *targets, const int *ctrl_offsets,

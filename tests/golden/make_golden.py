@@ -35,6 +35,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+from oracle.ref_import import reference_root  # noqa: E402
+
 
 # ------------------------------------------------------------------ recorder
 
@@ -425,7 +427,7 @@ def gate_matrices(qgate):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default=os.environ.get('QGATE_REF_ROOT', '/root/reference'))
+    ap.add_argument('--ref', default=reference_root())
     args = ap.parse_args()
     from oracle.ref_import import import_reference
     qgate = import_reference(args.ref)

@@ -29,12 +29,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+from oracle.ref_import import reference_root  # noqa: E402
+
 N, LAYERS = 12, 12
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default=os.environ.get('QGATE_REF_ROOT', '/root/reference'))
+    ap.add_argument('--ref', default=reference_root())
     args = ap.parse_args()
     from oracle.ref_import import import_reference
     qgate = import_reference(args.ref)

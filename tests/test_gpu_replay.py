@@ -25,3 +25,23 @@ def test_replay_reference_trace(rt, name, dtype, fusion):
         nat.set_fusion(0)
     assert not stats.failures, stats.failures[:5]
     assert stats.sample_mismatch_outside_tol == 0
+
+
+@pytest.mark.parametrize('dtype', [np.float64, np.float32], ids=['c128', 'c64'])
+def test_replay_reference_traces_through_trace_replay(rt, dtype):
+    """Every trace replayed three times in a row with trace replay on (the
+    default): runs of gates that recur between observations are captured
+    into CUDA graphs the second time and replayed the third, and every
+    result still matches the reference's."""
+    from qgate_gb300 import _native as nat
+    nat.set_fusion(0)
+    nat.set_trace_replay(True)
+    nat.trace_stats(reset=True)
+    for name in replay.trace_names():
+        calls, arrays = replay.load_trace(name)
+        for _ in range(3):
+            stats = replay.replay(calls, arrays, rt, dtype)
+            assert not stats.failures, (name, stats.failures[:5])
+            assert stats.sample_mismatch_outside_tol == 0, name
+    st = nat.trace_stats(reset=True)
+    assert st['captures'] > 0 and st['hits'] > 0, st

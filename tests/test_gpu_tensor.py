@@ -1,6 +1,7 @@
 """GPU parity of the tensor-core stage kernel (k_tstage): complex64 stages of
 12- and 13-lane tiles run as fused 5-lane blocks, each a 32x32 complex
-matrix applied by tcgen05 products in 3xTF32.
+matrix applied by tcgen05 kind::f16 products on split FP16 operands (FP32
+accumulation).
 
 Against the oracle's complex128 run: max amplitude error < 1e-5 and
 fidelity error |1 - <psi64|psi32>| < 1e-5 (the complex64 bound of the
