@@ -170,3 +170,70 @@ def test_tensor_stage_no_norm_drift_over_many_blocks(rt, tensor_mode):
         assert ferr < 3e-6 and abs(1. - norm) < 3e-6, (ferr, norm)
     assert nat.timing_read('tstage')[0] > 0
     assert nat.tensor_stage_status() == 0
+
+
+def _family(name, rng, n, layers):
+    """Gate lists ('g', name, args, adjoint, target, controls) whose fused
+    blocks differ in structure from the random U3 + CX circuit."""
+    ops = []
+    if name == 'skewed':
+        # amplitudes spread over ~17 orders of magnitude (|k> ~ 0.99^(n-w) 0.17^w)
+        ops += [('g', 'RY', (0.35,), False, q, ()) for q in range(n)]
+    for _ in range(layers):
+        if name == 'dense_blocks':
+            # random 5-qubit groups, each a U3 layer, a CX chain and a U3 layer:
+            # dense 32x32 blocks
+            perm = [int(x) for x in rng.permutation(n)]
+            for k in range(0, n - 4, 5):
+                grp = perm[k:k + 5]
+                for _rep in range(2):
+                    ops += [('g', 'U', tuple(rng.uniform(0, 2 * np.pi, 3)), False, q, ())
+                            for q in grp]
+                    ops += [('g', 'X', (), False, grp[i + 1], (grp[i],)) for i in range(4)]
+        elif name == 'diagonal':
+            # Rz on every qubit, CU1 ladders, H on three qubits: mostly phase ops
+            ops += [('g', 'RZ', (float(rng.uniform(-np.pi, np.pi)),), False, q, ())
+                    for q in range(n)]
+            for _k in range(n):
+                a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+                ops.append(('g', 'U1', (float(rng.uniform(-np.pi, np.pi)),), False, a, (b,)))
+            ops += [('g', 'H', (), False, int(q), ()) for q in rng.choice(n, 3, replace=False)]
+        elif name == 'sparse':
+            # CX and Toffoli permutations with a U3 on two qubits: sparse blocks
+            for _k in range(n // 2):
+                a, b, c = (int(x) for x in rng.choice(n, 3, replace=False))
+                ops.append(('g', 'X', (), False, a, (b, c) if rng.random() < 0.3 else (b,)))
+            ops += [('g', 'U', tuple(rng.uniform(0, 2 * np.pi, 3)), False, int(q), ())
+                    for q in rng.choice(n, 2, replace=False)]
+        elif name == 'skewed':
+            ops += [('g', 'U', (float(rng.uniform(0, 0.3)), float(rng.uniform(0, 2 * np.pi)),
+                                float(rng.uniform(0, 2 * np.pi))), False, q, ()) for q in range(n)]
+            perm = rng.permutation(n)
+            ops += [('g', 'X', (), False, int(perm[2 * k + 1]), (int(perm[2 * k]),))
+                    for k in range(n // 2)]
+    return ops
+
+
+@pytest.mark.parametrize('family', ['dense_blocks', 'diagonal', 'sparse', 'skewed'])
+def test_tensor_stage_accuracy_by_block_family(rt, tensor_mode, family):
+    """24 qubits, 24 layers of block families other than the benchmark's
+    (dense Haar-like 5-qubit blocks, diagonal-heavy stages that become phase
+    ops, sparse permutation blocks, and a state whose amplitudes span ~17
+    orders of magnitude), complex64 on the tensor-core stages against the
+    oracle's C port in complex128 (cs_run_circuit).  Bars: fidelity error
+    |1 - |<psi64|psi32>|| <= 1e-5 and max |p32 - p64| <= 1e-7, the bars of the
+    headline circuit."""
+    from oracle import cpu_port
+    nat = tensor_mode
+    rng = np.random.default_rng({'dense_blocks': 51, 'diagonal': 52, 'sparse': 53,
+                                 'skewed': 54}[family])
+    n = 24
+    ops = _family(family, rng, n, 24)
+    st = cpu_port.State(n, np.complex128)
+    st.run([(sv.gate_matrix(nm, a), t, c) for _, nm, a, _, t, c in ops], 14)
+    got = _run(rt, n, ops).astype(np.complex128)
+    ferr = abs(1. - abs(np.vdot(st.psi, got)))
+    perr = float(np.max(np.abs(np.abs(st.psi) ** 2 - np.abs(got) ** 2)))
+    print('%s: fidelity error %.3e, max probability error %.3e' % (family, ferr, perr))
+    assert ferr <= 1e-5 and perr <= 1e-7, (family, ferr, perr)
+    assert nat.timing_read('tstage')[0] > 0 and nat.tensor_stage_status() == 0
