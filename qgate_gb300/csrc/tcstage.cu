@@ -1,6 +1,9 @@
 // Tensor-core stage kernel (complex64): a tile of m = 12 or 13 lanes stays
-// on chip while a sequence of fused 5-lane blocks, each a 32x32 complex
-// unitary, is applied to it as tcgen05 matrix products.
+// on chip while a sequence of ops is applied to it: fused 5-lane blocks, each
+// a 32x32 complex unitary, as tcgen05 matrix products (dense ops), and runs of
+// diagonal gates as one table of phases multiplied in registers (phase ops:
+// each thread multiplies its amplitudes by their entries, found through a
+// slot table like the operand slots below; the layout stays).
 //
 // For a block on tile lanes L[0..4] the tile is a 2^(m-5) x 32 complex matrix
 // V (row = the other m-5 lanes, column = the block's amplitude index); the
