@@ -686,27 +686,51 @@ def run_batch(args, nat):
     """4096 hardware-efficient-ansatz circuits of uneven size (n ~ U{8..20},
     depth ~ U{4..12}, Ry and Rz on every qubit then a CX ladder; default_rng(20)),
     complex64, sum_i <Z_i> per circuit in FP64: circuits per second of the
-    call (host planning + one CUDA graph) and of the graph alone."""
+    call (host planning + one CUDA graph) and of the graph alone, for the one
+    persistent launch (default) and for one launch per round, with the bytes
+    of the large circuits' stage passes per second."""
     from qgate_gb300.batch import hea_batch, pack, sum_z
     circuits = hea_batch(count=args.batch_circuits, seed=20)
     packed = pack(circuits)
-    sum_z(packed=packed)  # warm-up
-    nat.timing_all(reset=True)
-    nat.timing_enable(True)
-    t0 = time.perf_counter()
-    for _ in range(args.batch_steps):
-        out = sum_z(packed=packed)
-    dt = (time.perf_counter() - t0) / args.batch_steps
-    nat.timing_enable(False)
-    launches, gms = nat.timing_read('batch', reset=True)
-    gates = int(packed[1][-1])
+    peak, peak_kind = measured_peak_hbm()
+    res = {'workload': '%d circuits, n ~ U{8..20}, depth ~ U{4..12}, Ry+Rz layers + CX ladder, '
+                       'sum_i <Z_i> per circuit' % len(circuits),
+           'gates': int(packed[1][-1])}
     amps = sum((1 << n) * len(ops) for n, ops in circuits)
-    return {'workload': '%d circuits, n ~ U{8..20}, depth ~ U{4..12}, Ry+Rz layers + CX ladder, '
-                        'sum_i <Z_i> per circuit' % len(circuits),
-            'gates': gates, 'circuits_per_s': len(circuits) / dt, 'ms_per_batch': dt * 1e3,
-            'graph_ms': gms / max(1, launches), 'circuits_per_s_graph':
-                len(circuits) / (gms / max(1, launches) / 1e3),
-            'amplitude_updates_per_s': amps / dt, 'checksum': float(np.sum(out))}
+    for label, one in (('one_launch', 1), ('per_round_launches', 0)):
+        nat.call('qg_set_batch_one_launch', one)
+        sum_z(packed=packed)  # warm-up
+        nat.timing_all(reset=True)
+        nat.gate_stats(reset=True)
+        nat.timing_enable(True)
+        t0 = time.perf_counter()
+        for _ in range(args.batch_steps):
+            out = sum_z(packed=packed)
+        dt = (time.perf_counter() - t0) / args.batch_steps
+        nat.timing_enable(False)
+        launches, gms = nat.timing_read('batch', reset=True)
+        st = nat.gate_stats(reset=True)
+        gms /= max(1, launches)
+        stage_bytes = st['bytes'] / args.batch_steps
+        res[label] = {'circuits_per_s': len(circuits) / dt, 'ms_per_batch': dt * 1e3,
+                      'graph_ms': gms, 'circuits_per_s_graph': len(circuits) / (gms / 1e3),
+                      'amplitude_updates_per_s': amps / dt,
+                      'stage_passes': st['passes'] / args.batch_steps,
+                      'stage_pass_bytes': stage_bytes,
+                      'stage_pass_gbs': stage_bytes / (gms / 1e3) / 1e9,
+                      'checksum': float(np.sum(out))}
+    nat.call('qg_set_batch_one_launch', 1)
+    one = res['one_launch']
+    res.update({'circuits_per_s': one['circuits_per_s'], 'graph_ms': one['graph_ms'],
+                'circuits_per_s_graph': one['circuits_per_s_graph'],
+                'bound': 'instruction issue in the tile programs (interpreted register ops '
+                         'and shared-memory transposes), not memory: the large circuits\' '
+                         'stage passes (read + write of a 64 KB - 8 MB state) move %.0f GB/s, '
+                         '%.2f of the %.0f GB/s HBM copy peak (%s); circuits of <= 12 qubits '
+                         'never leave shared memory' % (one['stage_pass_gbs'],
+                                                        one['stage_pass_gbs'] / peak, peak,
+                                                        peak_kind)})
+    return res
 
 
 def observation_kernels(args, rt, nat, proc, qs, n, cs, dtype, Lane, abs2):

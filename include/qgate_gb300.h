@@ -296,6 +296,14 @@ int qg_adjoint_expectation(int prec, int n_qubits, const qg_circuit_op *ops, int
 int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
                    const qg_circuit_op *gates, double *out);
 
+/* Extension: how qg_batch_sum_z runs a batch: 1 (default) as one persistent
+ * launch over a device-side queue of work items (whole circuits of <= 12
+ * qubits, tiles of the larger circuits' stages round by round, chunks of
+ * their final sums), items that need earlier ones waiting on per-circuit
+ * counters; 0 as one launch per round of stages (circuits of <= 13 qubits
+ * resident per CTA).  No reference counterpart. */
+int qg_set_batch_one_launch(int on);
+
 /* ---- allocation-free variant ------------------------------------------- */
 
 /* No counterpart in the reference.  Pr(local_lane == 0) of a state held in

@@ -62,6 +62,7 @@ SIGNATURES = {
     'qg_set_fusion_params': [_i, _i, _i, _i],
     'qg_set_stage_pipelining': [_i],
     'qg_set_trace_replay': [_i],
+    'qg_set_batch_one_launch': [_i],
     'qg_trace_stats': [_i64p, _i64p, _i],
     'qg_set_tensor_blocks': [_i],
     'qg_tensor_stage_status': [_i, _ip],

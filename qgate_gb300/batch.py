@@ -1,10 +1,15 @@
 """Batched execution of many small circuits of uneven qubit counts.
 
 `sum_z(circuits)` runs every circuit from |0...0> (complex64) and returns
-sum_i <Z_i> per circuit, accumulated in FP64.  Circuits of up to 13 qubits
-are simulated entirely inside one CTA's shared memory / registers; larger
-ones advance one fused stage per round over a packed device arena; the whole
-batch is one recorded CUDA graph (C ABI: `qg_batch_sum_z`).
+sum_i <Z_i> per circuit, accumulated in FP64.  The whole batch is one
+persistent launch (inside a recorded CUDA graph) whose CTAs take work items
+from a device-side queue: circuits of up to 12 qubits are simulated entirely
+inside one CTA's shared memory / registers; larger ones advance one fused
+stage at a time over a packed device arena (an item = four tiles of one
+stage; the queue runs round by round over all large circuits), an item
+waiting until its circuit's previous stage is complete; the last items sum
+each large circuit's <Z_i> (C ABI: `qg_batch_sum_z`; `qg_set_batch_one_launch`
+selects the one-launch-per-round form instead).
 
     circuits = [(n_qubits, [(gate_name, args, target, controls), ...]), ...]
 """

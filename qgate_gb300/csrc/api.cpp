@@ -177,6 +177,9 @@ struct Device {
     int reg_lanes[3] = {0, 3, 4};  // complex128 (double-float registers): 3
     int cost_budget[3] = {0, 0, 0};
     bool pipelined = false;  // persistent double-buffered stage kernel (opt-in)
+    // batched circuits as one persistent launch over a work queue (default),
+    // or as one launch per round of stages
+    bool batch_one_launch = true;
     // Kernels may write results straight into the caller's (pageable) host
     // buffers where the device accesses pageable memory through the host
     // page tables (Grace + NVLink-C2C), which skips the pinned staging.
@@ -1495,6 +1498,12 @@ int qg_qubit_processor_apply_controlled_gate(qg_handle hp, const double *mat, qg
 
 // ------------------------------------------------------------ compiled circuits
 
+int qg_set_batch_one_launch(int on) {
+    QG_BEGIN
+    g_dev.batch_one_launch = on != 0;
+    QG_END
+}
+
 int qg_set_trace_replay(int on) {
     QG_BEGIN
     flush_all();
@@ -1897,6 +1906,10 @@ static void append_sets(const std::vector<std::vector<int>> &sets, int m, int rl
     for (auto &st : sets) sets_all.push_back(make_set_slots(st.data(), rl, m, kFP32));
 }
 
+// Tiles of one stage per work item (a power of two, so it divides the tile
+// count of every large circuit): one wait and one completion count per item.
+constexpr int kBatchTilesPerItem = 4;
+
 int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
                    const qg_circuit_op *gates, double *out) {
     QG_BEGIN
@@ -1946,7 +1959,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
             merge_runs(gl);
             std::vector<RegOp<float>> prog;
             std::vector<std::vector<int>> sets;
-            if (n <= 13) {
+            if (n <= (g_dev.batch_one_launch ? 12 : 13)) {
                 P.resident = true;
                 P.rl = n <= 9 ? 3 : (n <= 12 ? 4 : 5);
                 std::vector<const PendingGate *> ptrs;
@@ -1959,6 +1972,9 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
             } else {
                 P.rl = 4;
                 auto plan = plan_gate_stages(gl, n, 12, 4);
+                // a circuit without gates still takes one (empty) pass, which
+                // writes its |0...0> state
+                if (plan.empty()) plan.emplace_back((1ULL << 12) - 1, std::vector<const PendingGate *>{});
                 for (size_t r = 0; r < plan.size(); ++r) {
                     TileLanes tl = tile_lanes_of(plan[r].first, n);
                     build_program<float>(plan[r].second, tl, 4, prog, sets);
@@ -2007,6 +2023,8 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
             rc.nops = (int)P.ops.size();
             rc.sets_off = sets_base;
             rc.out_index = c;
+            rc.n = P.n;
+            rc.rl = P.rl;
             rc.pad = 0;
             res[P.n].push_back(rc);
         } else {
@@ -2061,12 +2079,124 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
         owned.push_back(d_out);
         float2 *arena = (float2 *)d.arena.alloc(std::max<long long>(arena_elems, 1) * sizeof(float2));
         owned.push_back(arena);
+        // The one-launch form: a work queue of every resident circuit, every
+        // (stage, tile) of the large circuits round by round, and the chunks
+        // of their final sums, for one persistent launch.
+        std::vector<BatchItem> items;
+        std::vector<ResidentCircuit> res_all;
+        std::vector<BigCircuit> bigs;
+        int *d_counters = nullptr;
+        unsigned *d_status = nullptr;
+        BatchItem *d_bitems = nullptr;
+        ResidentCircuit *d_res_all = nullptr;
+        BigCircuit *d_big = nullptr;
+        int ctas = 0;
+        if (d.batch_one_launch) {
+            for (int n = 8; n <= 13; ++n) res_all.insert(res_all.end(), res[n].begin(), res[n].end());
+            std::vector<int> big_rounds(nbig, 0), big_tiles(nbig, 0);
+            for (int b = 0; b < nbig; ++b) {
+                BigCircuit bc;
+                bc.off = big_off[b];
+                bc.n = big_n[b];
+                bc.out_index = big_idx[b];
+                bigs.push_back(bc);
+                big_tiles[b] = 1 << (big_n[b] - 12);
+            }
+            std::vector<int> stage_big(stages.size());
+            {
+                int b = -1;
+                long long last_off = -1;
+                for (size_t si = 0; si < stages.size(); ++si) {
+                    if (stages[si].state_off != last_off) {
+                        ++b;
+                        last_off = stages[si].state_off;
+                    }
+                    stage_big[si] = b;
+                    big_rounds[b] += 1;
+                }
+            }
+            // Queue order: round by round over all large circuits (a round's
+            // items wait only on the previous round of their own circuit,
+            // which is a whole round of every circuit earlier in the queue,
+            // so they rarely wait at all); the resident circuits are spread
+            // over the round boundaries, and a circuit's final sums follow
+            // the round after its last one.
+            std::vector<std::vector<int>> big_stage_list(nbig);
+            for (size_t si = 0; si < stages.size(); ++si)
+                big_stage_list[stage_big[si]].push_back((int)si);
+            const size_t nrounds = rounds.size();
+            const size_t res_per = nrounds ? (res_all.size() + nrounds - 1) / nrounds
+                                           : res_all.size();
+            size_t next_res = 0;
+            auto push_residents = [&](size_t count) {
+                for (size_t k = 0; k < count && next_res < res_all.size(); ++k, ++next_res) {
+                    BatchItem it;
+                    memset(&it, 0, sizeof(it));
+                    it.kind = 0;
+                    it.index = (int)next_res;
+                    it.dep = -1;
+                    items.push_back(it);
+                }
+            };
+            auto push_sums = [&](int b) {
+                for (int k = 0; k < (int)batch_sumz_partials(1); ++k) {
+                    BatchItem it;
+                    memset(&it, 0, sizeof(it));
+                    it.kind = 2;
+                    it.index = b;
+                    it.tile = k;
+                    it.dep = b;
+                    it.need = big_rounds[b] * big_tiles[b];
+                    items.push_back(it);
+                }
+            };
+            for (size_t r = 0; r <= nrounds; ++r) {
+                for (int b = 0; b < nbig; ++b) {
+                    if ((int)r < big_rounds[b]) {
+                        const int per = std::min(big_tiles[b], kBatchTilesPerItem);
+                        for (int t = 0; t < big_tiles[b]; t += per) {
+                            BatchItem it;
+                            memset(&it, 0, sizeof(it));
+                            it.kind = 1;
+                            it.index = big_stage_list[b][r];
+                            it.tile = t;
+                            it.ntiles = per;
+                            it.round = (int)r;
+                            it.dep = r > 0 ? b : -1;
+                            it.need = (int)r * big_tiles[b];
+                            it.dep_done = b;
+                            items.push_back(it);
+                        }
+                    } else if (r == std::min((size_t)big_rounds[b] + 1, nrounds)) {
+                        push_sums(b);
+                    }
+                }
+                push_residents(res_per);
+            }
+            push_residents(res_all.size());
+            d_bitems = (BatchItem *)up(items.data(), items.size() * sizeof(BatchItem));
+            d_res_all = (ResidentCircuit *)up(res_all.data(), res_all.size() * sizeof(ResidentCircuit));
+            d_big = (BigCircuit *)up(bigs.data(), bigs.size() * sizeof(BigCircuit));
+            d_counters = (int *)d.arena.alloc(sizeof(int) * (1 + 2 * (size_t)nbig) + 16);
+            owned.push_back(d_counters);
+            d_status = (unsigned *)d.arena.alloc(16);
+            owned.push_back(d_status);
+            ctas = batch_persistent_ctas();
+        }
         batch_prepare();
         QG_CUDA(cudaStreamSynchronize(d.stream));
 
         // Record the whole batch as one CUDA graph, then launch it.
         QG_CUDA(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
         try {
+            if (d.batch_one_launch) {
+                QG_CUDA(cudaMemsetAsync(d_counters, 0, sizeof(int) * (1 + 2 * (size_t)nbig),
+                                        d.stream));
+                QG_CUDA(cudaMemsetAsync(d_status, 0, sizeof(unsigned), d.stream));
+                launch_batch_persistent(d_bitems, (int)items.size(), d_counters, nbig, d_status,
+                                        d_res_all, d_stages, d_ops, d_sets, arena, d_big, d_part,
+                                        d_out, ctas, d.stream);
+            } else {
             if (arena_elems)
                 QG_CUDA(cudaMemsetAsync(arena, 0, arena_elems * sizeof(float2), d.stream));
             launch_batch_init(arena, d_off, nbig, d.stream);
@@ -2077,6 +2207,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                 launch_batch_stage(d_stages, d_items + round_off[r], (int)rounds[r].size(), d_ops,
                                    d_sets, arena, d.stream);
             launch_batch_sumz(arena, d_off, d_n, d_idx, nbig, d_part, d_out, d.stream);
+            }
         } catch (...) {
             cudaStreamEndCapture(d.stream, &graph);
             throw;
@@ -2084,9 +2215,20 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
         QG_CUDA(cudaStreamEndCapture(d.stream, &graph));
         QG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
         timed(d, "batch", [&] { QG_CUDA(cudaGraphLaunch(exec, d.stream)); });
+        // stage passes of the large circuits (each a read and a write of the
+        // state, through L2 where it fits) for the caller's statistics
+        for (const BatchStage &st : stages) {
+            d.n_passes += 1;
+            d.n_bytes += 2 * ((long long)1 << st.n) * (long long)sizeof(float2);
+        }
         QG_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * n_circuits, cudaMemcpyDeviceToHost,
                                 d.stream));
+        unsigned status = 0;
+        if (d_status)
+            QG_CUDA(cudaMemcpyAsync(&status, d_status, sizeof(status), cudaMemcpyDeviceToHost,
+                                    d.stream));
         QG_CUDA(cudaStreamSynchronize(d.stream));
+        if (status) fail(QG_ERR_TIMEOUT, "batch: a bounded wait of the persistent launch gave up.");
     } catch (...) {
         cudaStreamSynchronize(d.stream);
         if (exec) cudaGraphExecDestroy(exec);

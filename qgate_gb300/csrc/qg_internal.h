@@ -273,7 +273,21 @@ struct BatchStage {
 // whole gate program, then sum_i <Z_i> (FP64) to out[circuit].
 struct ResidentCircuit {
     long long ops_off;
-    int nops, sets_off, out_index, pad;
+    int nops, sets_off, out_index, n, rl, pad;
+};
+// A large circuit of a batch: its state's element offset in the arena, its
+// qubits, and where its result goes.
+struct BigCircuit {
+    long long off;
+    int n, out_index;
+};
+// A work item of the one-launch batch: kind 0 = resident circuit res[index];
+// kind 1 = tiles [tile, tile + ntiles) of stage stages[index] (round
+// `round`; it adds ntiles to done[dep_done] when finished); kind 2 = chunk
+// `tile` of big[index]'s final sum.  It waits until done[dep] >= need first
+// (dep = -1: no wait).
+struct BatchItem {
+    int kind, index, tile, round, dep, need, dep_done, ntiles;
 };
 
 void launch_batch_resident(int n, int rl, const ResidentCircuit *d_circuits, int count,
@@ -292,6 +306,16 @@ void launch_batch_sumz(const float2 *arena, const long long *d_off, const int *d
                        cudaStream_t stream);
 void launch_batch_init(float2 *arena, const long long *d_off, int count, cudaStream_t stream);
 void batch_prepare();
+// The whole batch as one persistent (cooperative) launch of `ctas` CTAs over
+// the work items; d_counters: 1 + 2 n_big zeroed ints; *d_status nonzero if a
+// bounded wait gave up; partials: batch_sumz_partials(n_big) doubles.
+void launch_batch_persistent(const BatchItem *d_items, int n_items, int *d_counters,
+                             int n_big, unsigned *d_status, const ResidentCircuit *d_res,
+                             const BatchStage *d_stages, const RegOp<float> *d_ops,
+                             const SetSlots *d_sets, float2 *arena, const BigCircuit *d_big,
+                             double *d_partials, double *d_out, int ctas, cudaStream_t stream);
+// CTAs of the persistent launch that fit on the device at once.
+int batch_persistent_ctas();
 
 // Engine services for other translation units.
 cudaStream_t engine_stream();

@@ -43,3 +43,46 @@ def test_batch_repeatable_and_order_independent():
     a = sum_z(circuits)
     b = sum_z(circuits[::-1])[::-1]
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize('one_launch', [1, 0], ids=['one_launch', 'per_round'])
+def test_batch_circuits_without_gates(one_launch):
+    """Circuits with no gates, resident (10 qubits) and staged (15 qubits),
+    beside ones with gates: sum_i <Z_i> of |0...0> is n."""
+    from qgate_gb300 import _native as nat
+    from qgate_gb300.batch import hea_batch, sum_z
+    circuits = [(10, []), (15, [])] + hea_batch(count=6, seed=8, min_qubits=13, max_qubits=16)
+    nat.call('qg_set_batch_one_launch', one_launch)
+    try:
+        got = sum_z(circuits)
+    finally:
+        nat.call('qg_set_batch_one_launch', 1)
+    assert got[0] == 10.0 and got[1] == 15.0, got[:2]
+    for (n, ops), a in zip(circuits[2:], got[2:]):
+        want = _oracle_sum_z(n, ops)
+        assert abs(a - want) < 2e-5 * n, (n, a, want)
+
+
+def test_batch_one_launch_equals_per_round_launches():
+    """The batch as one persistent launch over the work queue (default) and as
+    one launch per round give the same sums (both against the oracle), for the
+    benchmark's mix of 8..20-qubit circuits; the one-launch path ran (a
+    single timed launch per call)."""
+    from qgate_gb300 import _native as nat
+    from qgate_gb300.batch import hea_batch, sum_z
+    circuits = hea_batch(count=48, seed=5, min_qubits=8, max_qubits=20, min_depth=2,
+                         max_depth=8)
+    nat.timing_enable(True)
+    nat.timing_read('', reset=True)
+    one = sum_z(circuits)
+    launches, _ = nat.timing_read('batch', reset=True)
+    nat.timing_enable(False)
+    assert launches == 1
+    nat.call('qg_set_batch_one_launch', 0)
+    try:
+        per_round = sum_z(circuits)
+    finally:
+        nat.call('qg_set_batch_one_launch', 1)
+    for (n, ops), a, b in zip(circuits, one, per_round):
+        want = _oracle_sum_z(n, ops)
+        assert abs(a - want) < 2e-5 * n and abs(b - want) < 2e-5 * n, (n, a, b, want)
