@@ -5,8 +5,8 @@ sum_i <Z_i> per circuit, accumulated in FP64.  The whole batch is one
 persistent launch (inside a recorded CUDA graph) whose CTAs take work items
 from a device-side queue: circuits of up to 12 qubits are simulated entirely
 inside one CTA's shared memory / registers; larger ones advance one fused
-stage at a time over a packed device arena (an item = four tiles of one
-stage; the queue runs round by round over all large circuits), an item
+stage at a time over a packed device arena (an item = up to eight tiles of
+one stage; the queue runs round by round over all large circuits), an item
 waiting until its circuit's previous stage is complete; the last items sum
 each large circuit's <Z_i> (C ABI: `qg_batch_sum_z`; `qg_set_batch_one_launch`
 selects the one-launch-per-round form instead).

@@ -1906,9 +1906,30 @@ static void append_sets(const std::vector<std::vector<int>> &sets, int m, int rl
     for (auto &st : sets) sets_all.push_back(make_set_slots(st.data(), rl, m, kFP32));
 }
 
+// k with a 0 bit inserted at each of pos[0..npos) in turn (the host copy of
+// the kernels' tile-index to amplitude-index map).
+static unsigned long long host_insert_zeros(unsigned long long k, const int *pos, int npos) {
+    for (int i = 0; i < npos; ++i) {
+        const unsigned long long low = k & ((1ULL << pos[i]) - 1);
+        k = ((k ^ low) << 1) | low;
+    }
+    return k;
+}
+
+// The bits of k placed, in order, at the set bits of mask.
+static unsigned host_deposit(unsigned k, unsigned mask) {
+    unsigned r = 0;
+    for (unsigned b = 1; mask; b <<= 1) {
+        const unsigned low = mask & (0u - mask);
+        if (k & b) r |= low;
+        mask ^= low;
+    }
+    return r;
+}
+
 // Tiles of one stage per work item (a power of two, so it divides the tile
 // count of every large circuit): one wait and one completion count per item.
-constexpr int kBatchTilesPerItem = 4;
+constexpr int kBatchTilesPerItem = 8;
 
 int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
                    const qg_circuit_op *gates, double *out) {
@@ -1919,6 +1940,11 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
     // Plan every circuit independently (in parallel), then concatenate.
     struct StagePart {
         BatchStage hdr;  // ops_off / sets_off local to the circuit
+        // Tile-index bits that can be 1 in a tile with a nonzero amplitude:
+        // the run starts from |0...0>, so before this stage every amplitude
+        // whose lanes outside the earlier stages' tiles are not all 0 is
+        // still 0 (a stage mixes amplitudes only within its tiles).
+        unsigned live;
     };
     struct Plan {
         int n = 0, rl = 0;
@@ -1975,6 +2001,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                 // a circuit without gates still takes one (empty) pass, which
                 // writes its |0...0> state
                 if (plan.empty()) plan.emplace_back((1ULL << 12) - 1, std::vector<const PendingGate *>{});
+                unsigned long long support = 0;  // lanes of the stages so far
                 for (size_t r = 0; r < plan.size(); ++r) {
                     TileLanes tl = tile_lanes_of(plan[r].first, n);
                     build_program<float>(plan[r].second, tl, 4, prog, sets);
@@ -1989,6 +2016,11 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                     sp.hdr.nops = (int)prog.size();
                     sp.hdr.ops_off = (long long)P.ops.size();
                     sp.hdr.sets_off = (int)P.sets.size();
+                    sp.live = 0;
+                    for (int i = 0; i < n - 12; ++i)
+                        if (host_insert_zeros(1ULL << i, sp.hdr.ins_pos, sp.hdr.nins) & support)
+                            sp.live |= 1u << i;
+                    support |= plan[r].first;
                     P.ops.insert(P.ops.end(), prog.begin(), prog.end());
                     append_sets(sets, 12, 4, P.sets);
                     P.stages.push_back(sp);
@@ -2007,6 +2039,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
     std::vector<SetSlots> sets_all;
     std::vector<ResidentCircuit> res[14];
     std::vector<BatchStage> stages;
+    std::vector<unsigned> stage_live;
     std::vector<std::vector<int2>> rounds;
     std::vector<long long> big_off;
     std::vector<int> big_n, big_idx;
@@ -2040,9 +2073,13 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                 st.sets_off += sets_base;
                 int sidx = (int)stages.size();
                 stages.push_back(st);
+                stage_live.push_back(P.stages[r].live);
                 if (rounds.size() <= r) rounds.resize(r + 1);
-                for (long long t = 0; t < (1LL << (P.n - 12)); ++t)
-                    rounds[r].push_back(make_int2(sidx, (int)t));
+                // the per-round form starts from a zeroed arena: only the
+                // tiles that can hold a nonzero amplitude run
+                const unsigned live = P.stages[r].live;
+                for (unsigned k = 0; k < (1u << __builtin_popcount(live)); ++k)
+                    rounds[r].push_back(make_int2(sidx, (int)host_deposit(k, live)));
             }
         }
     }
@@ -2124,6 +2161,21 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
             std::vector<std::vector<int>> big_stage_list(nbig);
             for (size_t si = 0; si < stages.size(); ++si)
                 big_stage_list[stage_big[si]].push_back((int)si);
+            // Tiles each stage runs: round 0 writes every tile (the arena is
+            // not cleared; tiles other than tile 0 just store zeros), later
+            // rounds only the tiles that can hold a nonzero amplitude.
+            // done[] of a circuit counts run tiles; before round r it must
+            // reach the sum over its earlier rounds.
+            std::vector<std::vector<int>> big_need(nbig);
+            for (int b = 0; b < nbig; ++b) {
+                int acc = 0;
+                for (size_t r = 0; r < big_stage_list[b].size(); ++r) {
+                    big_need[b].push_back(acc);
+                    acc += r == 0 ? big_tiles[b]
+                                  : 1 << __builtin_popcount(stage_live[big_stage_list[b][r]]);
+                }
+                big_need[b].push_back(acc);
+            }
             const size_t nrounds = rounds.size();
             const size_t res_per = nrounds ? (res_all.size() + nrounds - 1) / nrounds
                                            : res_all.size();
@@ -2146,24 +2198,28 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                     it.index = b;
                     it.tile = k;
                     it.dep = b;
-                    it.need = big_rounds[b] * big_tiles[b];
+                    it.need = big_need[b][big_rounds[b]];
                     items.push_back(it);
                 }
             };
             for (size_t r = 0; r <= nrounds; ++r) {
                 for (int b = 0; b < nbig; ++b) {
                     if ((int)r < big_rounds[b]) {
-                        const int per = std::min(big_tiles[b], kBatchTilesPerItem);
-                        for (int t = 0; t < big_tiles[b]; t += per) {
+                        const int si = big_stage_list[b][r];
+                        const unsigned live = r == 0 ? (unsigned)big_tiles[b] - 1u : stage_live[si];
+                        const int count = 1 << __builtin_popcount(live);
+                        const int per = std::min(count, kBatchTilesPerItem);
+                        for (int t = 0; t < count; t += per) {
                             BatchItem it;
                             memset(&it, 0, sizeof(it));
                             it.kind = 1;
-                            it.index = big_stage_list[b][r];
+                            it.index = si;
                             it.tile = t;
                             it.ntiles = per;
+                            it.live = live;
                             it.round = (int)r;
                             it.dep = r > 0 ? b : -1;
-                            it.need = (int)r * big_tiles[b];
+                            it.need = big_need[b][r];
                             it.dep_done = b;
                             items.push_back(it);
                         }
@@ -2217,9 +2273,14 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
         timed(d, "batch", [&] { QG_CUDA(cudaGraphLaunch(exec, d.stream)); });
         // stage passes of the large circuits (each a read and a write of the
         // state, through L2 where it fits) for the caller's statistics
-        for (const BatchStage &st : stages) {
+        for (size_t si = 0; si < stages.size(); ++si) {
+            const long long tile_bytes = (long long)sizeof(float2) << 12;
+            const long long run = 1LL << __builtin_popcount(stage_live[si]);
             d.n_passes += 1;
-            d.n_bytes += 2 * ((long long)1 << st.n) * (long long)sizeof(float2);
+            d.n_bytes += 2 * run * tile_bytes;
+            // round 0 of the one-launch form also stores the zero tiles
+            if (d.batch_one_launch && stage_live[si] == 0)
+                d.n_bytes += (((long long)1 << (stages[si].n - 12)) - 1) * tile_bytes;
         }
         QG_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * n_circuits, cudaMemcpyDeviceToHost,
                                 d.stream));

@@ -267,6 +267,17 @@ __device__ __forceinline__ double resident_sum_z(const ResidentCircuit &c, C *sm
     return block_sum_d((double)part, ws);
 }
 
+// The bits of k placed, in order, at the set bits of mask.
+__device__ __forceinline__ int deposit(int k, unsigned mask) {
+    unsigned r = 0;
+    for (unsigned b = 1; mask; b <<= 1) {
+        const unsigned low = mask & (0u - mask);
+        if ((unsigned)k & b) r |= low;
+        mask ^= low;
+    }
+    return (int)r;
+}
+
 // The whole batch in one persistent launch.  CTAs take work items in queue
 // order (an atomic head): a whole small circuit (resident in shared memory),
 // a run of tiles of one fused stage of a large circuit (in the arena), or one
@@ -337,10 +348,18 @@ k_batch_persistent(const BatchItem *__restrict__ items, int n_items, int *head, 
                                   &s[base | dt | st.dep_hi[i]]);
                 asm volatile("cp.async.commit_group;\n" ::: "memory");
             };
-            if (w.round > 0) load_tile(sm, w.tile);
+            if (w.round > 0) load_tile(sm, deposit(w.tile, w.live));
             for (int j = 0; j < w.ntiles; ++j) {
                 C *cur = sm + ((j & 1) << 12);
-                const int tile = w.tile + j;
+                const int tile = deposit(w.tile + j, w.live);
+                if (w.round == 0 && tile != 0) {
+                    // round 0 from |0...0>: every tile but tile 0 stays zero
+                    const idx_t base = insert_zeros((idx_t)tile, st.ins_pos, st.nins);
+#pragma unroll
+                    for (int i = 0; i < NR; ++i)
+                        __stcg(&s[base | dt | st.dep_hi[i]], make_float2(0.f, 0.f));
+                    continue;
+                }
                 if (w.round == 0) {
                     // |0...0>: only element 0 of tile 0 is 1 (its slot is 0)
 #pragma unroll
@@ -349,7 +368,7 @@ k_batch_persistent(const BatchItem *__restrict__ items, int n_items, int *head, 
                     __syncthreads();
                     if (tile == 0 && tid == 0) cur[0] = make_float2(1.f, 0.f);
                 } else if (j + 1 < w.ntiles) {
-                    load_tile(sm + (((j + 1) & 1) << 12), tile + 1);
+                    load_tile(sm + (((j + 1) & 1) << 12), deposit(w.tile + j + 1, w.live));
                     asm volatile("cp.async.wait_group 1;\n" ::: "memory");
                 } else {
                     asm volatile("cp.async.wait_group 0;\n" ::: "memory");

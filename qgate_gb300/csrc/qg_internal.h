@@ -282,12 +282,15 @@ struct BigCircuit {
     int n, out_index;
 };
 // A work item of the one-launch batch: kind 0 = resident circuit res[index];
-// kind 1 = tiles [tile, tile + ntiles) of stage stages[index] (round
-// `round`; it adds ntiles to done[dep_done] when finished); kind 2 = chunk
-// `tile` of big[index]'s final sum.  It waits until done[dep] >= need first
-// (dep = -1: no wait).
+// kind 1 = tiles k = tile .. tile + ntiles - 1 of stage stages[index] (round
+// `round`), where k counts the tiles whose index bits lie in `live` (tile
+// index = the bits of k deposited at the set bits of live); it adds ntiles to
+// done[dep_done] when finished; kind 2 = chunk `tile` of big[index]'s final
+// sum.  It waits until done[dep] >= need first (dep = -1: no wait).
 struct BatchItem {
     int kind, index, tile, round, dep, need, dep_done, ntiles;
+    unsigned live;
+    int pad[3];
 };
 
 void launch_batch_resident(int n, int rl, const ResidentCircuit *d_circuits, int count,

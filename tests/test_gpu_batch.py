@@ -37,6 +37,37 @@ def test_batch_mixed_gates_and_controls():
         assert abs(g - _oracle_sum_z(n, ops)) < 2e-5 * n
 
 
+@pytest.mark.parametrize('one_launch', [1, 0], ids=['one_launch', 'per_round'])
+def test_batch_support_growing_over_many_stages(one_launch):
+    """Circuits whose nonzero amplitudes spread over the lanes a few at a
+    time (gates on the low lanes first, then entangling gates that reach one
+    more high lane per stage), so that the stages skip different sets of
+    tiles that can still only hold zeros; against the oracle."""
+    from qgate_gb300 import _native as nat
+    from qgate_gb300.batch import sum_z
+    rng = np.random.default_rng(31)
+    circuits = []
+    for n in (14, 17, 19):
+        ops = [('H', (), q, ()) for q in range(12)]
+        for hi in range(12, n):
+            lo = int(rng.integers(0, 12))
+            ops.append(('RY', (float(rng.uniform(0, 3)),), lo, ()))
+            ops.append(('X', (), hi, (lo,)))
+            ops.append(('RZ', (float(rng.uniform(0, 3)),), hi, ()))
+            # a wide gate on low lanes between, so that the next high lane
+            # lands in a later stage
+            ops += [('X', (), q + 1, (q,)) for q in range(11)]
+        circuits.append((n, ops))
+    nat.call('qg_set_batch_one_launch', one_launch)
+    try:
+        got = sum_z(circuits)
+    finally:
+        nat.call('qg_set_batch_one_launch', 1)
+    for (n, ops), g in zip(circuits, got):
+        want = _oracle_sum_z(n, ops)
+        assert abs(g - want) < 2e-5 * n, (n, g, want)
+
+
 def test_batch_repeatable_and_order_independent():
     from qgate_gb300.batch import hea_batch, sum_z
     circuits = hea_batch(count=40, seed=4, max_qubits=16)
