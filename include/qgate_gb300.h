@@ -304,6 +304,13 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
  * resident per CTA).  No reference counterpart. */
 int qg_set_batch_one_launch(int on);
 
+/* Extension: counters of the qubit-grouping policy, in this order: join
+ * calls, kron passes, state buffers allocated, decohere_and_separate calls,
+ * separations formed in place, separations formed by copy, copies of a
+ * buffer still read by a lazy states object before a write.  Writes the
+ * first min(n, 7); reset != 0 zeroes them.  No reference counterpart. */
+int qg_grouping_stats(int64_t *out, int n, int reset);
+
 /* ---- allocation-free variant ------------------------------------------- */
 
 /* No counterpart in the reference.  Pr(local_lane == 0) of a state held in

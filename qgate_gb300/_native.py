@@ -63,6 +63,7 @@ SIGNATURES = {
     'qg_set_stage_pipelining': [_i],
     'qg_set_trace_replay': [_i],
     'qg_set_batch_one_launch': [_i],
+    'qg_grouping_stats': [_i64p, _i, _i],
     'qg_trace_stats': [_i64p, _i64p, _i],
     'qg_set_tensor_blocks': [_i],
     'qg_tensor_stage_status': [_i, _ip],
@@ -181,6 +182,18 @@ def trace_stats(reset=False):
     h, c = _i64(0), _i64(0)
     check(lib.qg_trace_stats(ctypes.byref(h), ctypes.byref(c), 1 if reset else 0))
     return {'hits': h.value, 'captures': c.value}
+
+
+GROUPING_KEYS = ('joins', 'krons', 'allocs', 'separates', 'inplace', 'copies', 'cow')
+
+
+def grouping_stats(reset=False):
+    """Counters of the qubit-grouping policy: join calls, kron passes, state
+    buffers allocated, decohere_and_separate calls, separations formed in
+    place / by copy, copies of buffers still read by a lazy object."""
+    out = np.zeros(len(GROUPING_KEYS), np.int64)
+    check(lib.qg_grouping_stats(out.ctypes.data_as(_i64p), len(out), 1 if reset else 0))
+    return dict(zip(GROUPING_KEYS, (int(x) for x in out)))
 
 
 def tensor_stage_status(reset=False):

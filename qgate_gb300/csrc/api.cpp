@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <set>
 #include <unordered_map>
@@ -112,12 +113,53 @@ struct Arena {
 
 // ------------------------------------------------------------ objects
 
+// A device buffer of amplitudes.  Shared between a states object and the
+// lazy states objects that read it (a product formed by join, a view left by
+// decohere_and_separate); returned to the arena when the last holder drops it.
+struct Buf {
+    void *d = nullptr;
+    size_t bytes = 0;
+    Buf() = default;
+    Buf(const Buf &) = delete;
+    Buf &operator=(const Buf &) = delete;
+    ~Buf();
+};
+typedef std::shared_ptr<Buf> BufPtr;
+
+// One factor of a lazy product: a buffer of 2^n_lanes amplitudes, or (buf
+// null) the basis state |basis> on n_lanes lanes.
+struct Factor {
+    BufPtr buf;
+    int n_lanes = 0;
+    long long basis = 0;
+};
+
+// Qubit-grouping policy.  The front-end allocates, joins and separates
+// states objects as its qubit groups change (qgate/simulator/
+// qubits_handler.py:34-122); the amplitudes are formed only when something
+// reads them:
+//  - initialize / reset leave a product of one basis factor (no buffer yet);
+//  - join leaves a product of the sources' buffers (shared, not copied) and
+//    their pending gates moved up to the joined lanes: a chain of joins
+//    between two reads costs one kron pass, or none when every factor is
+//    still a basis state (the joined gates then run on a fresh |0...0>);
+//  - decohere_and_separate leaves the remaining lanes as a view of the
+//    source's buffer; when it is read and the source is gone, the lane is
+//    removed in place and the view adopts the buffer (no allocation).
+// A buffer shared with a lazy object is copied before it is written.
 struct States {
     int prec;
     int n_lanes = -1;
-    void *d = nullptr;
+    void *d = nullptr;  // buf->d once materialized
+    BufPtr buf;
     std::vector<PendingGate> pending;
     bool streamed = false;  // part of the pending run was launched by the streaming flush
+    enum { kDense = 0, kProduct = 1, kView = 2 };
+    int lazy = kDense;
+    std::vector<Factor> factors;  // kProduct: the last factor at the lowest lanes
+    BufPtr parent;                // kView: the n_lanes + 1 lane source
+    int sep_lane = 0, sep_value = 0;
+    double sep_norm = 1.;
 };
 
 struct Processor {
@@ -202,6 +244,11 @@ struct Device {
     unsigned char *h_bring = nullptr, *d_bring = nullptr;
     size_t bring_off = 0;
     long long n_gates = 0, n_passes = 0, n_bytes = 0;
+    // qubit-grouping counters: join calls, kron passes, state buffers
+    // allocated, decohere_and_separate calls, separations done in place / by
+    // copy, copies of shared buffers before a write
+    long long g_joins = 0, g_krons = 0, g_allocs = 0, g_separates = 0, g_inplace = 0,
+              g_copies = 0, g_cow = 0;
     // Per-kernel-class launch timing with CUDA events on the engine's stream.
     bool timing = false;
     struct TimedClass {
@@ -258,6 +305,8 @@ static void device_init(int device_id, long long limit) {
     d.initialized = true;
 }
 
+Buf::~Buf() { g_dev.arena.release(d); }
+
 static Device &dev() {
     if (!g_dev.initialized) device_init(-1, -1);
     QG_CUDA(cudaSetDevice(g_dev.dev));
@@ -277,7 +326,7 @@ template <class T> static T *lookup(std::unordered_set<T *> &set, qg_handle h, c
 static States *get_states(qg_handle h) { return lookup(g_dev.states, h, "qubit states"); }
 static States *get_alloc_states(qg_handle h) {
     States *s = get_states(h);
-    if (!s->d) fail(QG_ERR_RUNTIME, "qubit states not initialized.");
+    if (!s->d && s->lazy == States::kDense) fail(QG_ERR_RUNTIME, "qubit states not initialized.");
     return s;
 }
 
@@ -309,6 +358,144 @@ template <class F> static void timed(Device &d, const char *cls, F launch) {
     launch();
     QG_CUDA(cudaEventRecord(b, d.stream));
     d.timers[cls].pending.emplace_back(a, b);
+}
+
+// ------------------------------------------------------------ grouping
+
+static PairIdx pair_pattern(const std::vector<int> &fixed, unsigned long long set_mask,
+                            unsigned long long partner);
+
+static BufPtr new_buffer(Device &d, int prec, int n_lanes) {
+    BufPtr b = std::make_shared<Buf>();
+    b->bytes = ((size_t)1 << n_lanes) * complex_size(prec);
+    b->d = d.arena.alloc(b->bytes);
+    d.g_allocs += 1;
+    return b;
+}
+
+static void set_buffer(States *s, BufPtr b) {
+    s->buf = std::move(b);
+    s->d = s->buf ? s->buf->d : nullptr;
+}
+
+// Forget the amplitudes (not the pending gates or the lane count).
+static void drop_contents(States *s) {
+    set_buffer(s, nullptr);
+    s->lazy = States::kDense;
+    s->factors.clear();
+    s->parent.reset();
+}
+
+static void set_basis(States *s, long long basis) {
+    drop_contents(s);
+    s->lazy = States::kProduct;
+    Factor f;
+    f.n_lanes = s->n_lanes;
+    f.basis = basis;
+    s->factors.push_back(f);
+}
+
+// Adjacent basis factors multiply to one basis factor.
+static void coalesce_factors(std::vector<Factor> &fs) {
+    std::vector<Factor> out;
+    for (auto &f : fs) {
+        if (!f.buf && !out.empty() && !out.back().buf) {
+            out.back().basis = (out.back().basis << f.n_lanes) | f.basis;
+            out.back().n_lanes += f.n_lanes;
+        } else {
+            out.push_back(f);
+        }
+    }
+    fs.swap(out);
+}
+
+// Kron of factors (the last at the lowest lanes) into a fresh buffer.
+static BufPtr kron_factors(Device &d, int prec, std::vector<Factor> fs) {
+    while ((int)fs.size() > kMaxGetterStates) {
+        // the lowest factors first into one buffer
+        std::vector<Factor> low(fs.end() - kMaxGetterStates, fs.end());
+        fs.resize(fs.size() - kMaxGetterStates);
+        Factor f;
+        for (auto &x : low) f.n_lanes += x.n_lanes;
+        f.buf = kron_factors(d, prec, low);
+        fs.push_back(f);
+    }
+    int n = 0;
+    std::vector<const void *> srcs;
+    std::vector<int> lanes;
+    std::vector<long long> basis;
+    for (auto &f : fs) {
+        srcs.push_back(f.buf ? f.buf->d : nullptr);
+        lanes.push_back(f.n_lanes);
+        basis.push_back(f.basis);
+        n += f.n_lanes;
+    }
+    BufPtr b = new_buffer(d, prec, n);
+    bool any_buffer = false;
+    for (auto &f : fs) any_buffer = any_buffer || f.buf != nullptr;
+    if (fs.size() == 1 && !fs[0].buf && fs[0].basis == 0) {
+        timed(d, "init", [&] { launch_init_basis(prec, b->d, (idx_t)1 << n, d.stream); });
+    } else if (!any_buffer) {
+        // a basis state: written, nothing read
+        timed(d, "init", [&] {
+            launch_kron(prec, b->d, (idx_t)1 << n, srcs.data(), lanes.data(), (int)srcs.size(),
+                        d.stream, basis.data());
+        });
+    } else {
+        d.g_krons += 1;
+        timed(d, "join", [&] {
+            launch_kron(prec, b->d, (idx_t)1 << n, srcs.data(), lanes.data(), (int)srcs.size(),
+                        d.stream, basis.data());
+        });
+    }
+    return b;
+}
+
+// Forms the amplitudes of a lazy states object (its pending gates stay
+// pending).
+static void materialize(Device &d, States *s) {
+    if (s->lazy == States::kProduct) {
+        BufPtr b = kron_factors(d, s->prec, s->factors);
+        s->factors.clear();
+        s->lazy = States::kDense;
+        set_buffer(s, b);
+    } else if (s->lazy == States::kView) {
+        BufPtr par = s->parent;
+        s->parent.reset();
+        s->lazy = States::kDense;
+        if (par.use_count() == 1) {
+            // the source is gone: remove the lane in place and keep its buffer
+            d.g_inplace += 1;
+            timed(d, "measure", [&] {
+                launch_shrink_inplace(s->prec, par->d, s->n_lanes + 1, s->sep_lane, s->sep_value,
+                                      s->sep_norm, d.stream);
+            });
+            set_buffer(s, par);
+        } else {
+            d.g_copies += 1;
+            BufPtr b = new_buffer(d, s->prec, s->n_lanes);
+            PairIdx pi = pair_pattern({s->sep_lane}, (unsigned long long)s->sep_value << s->sep_lane,
+                                      0);
+            timed(d, "measure", [&] {
+                launch_shrink(s->prec, b->d, par->d, (idx_t)1 << s->n_lanes, pi, s->sep_norm,
+                              d.stream);
+            });
+            set_buffer(s, b);
+        }
+    }
+}
+
+// Materializes s and makes its buffer its own (copied if a lazy object still
+// reads it), before an in-place write.
+static void prepare_write(Device &d, States *s) {
+    materialize(d, s);
+    if (s->buf && s->buf.use_count() > 1) {
+        d.g_cow += 1;
+        BufPtr b = new_buffer(d, s->prec, s->n_lanes);
+        QG_CUDA(cudaMemcpyAsync(b->d, s->d, ((size_t)1 << s->n_lanes) * complex_size(s->prec),
+                                cudaMemcpyDeviceToDevice, d.stream));
+        set_buffer(s, b);
+    }
 }
 
 static void settle_timers(Device &d) {
@@ -732,6 +919,7 @@ static void stream_flush(States *s) {
     int M;
     unsigned long long base;
     if (s->pending.size() < kStreamAt || !lookahead_params(d, s, M, base)) return;
+    prepare_write(d, s);
     merge_runs(s->pending);
     std::vector<const PendingGate *> remaining;
     for (auto &g : s->pending) remaining.push_back(&g);
@@ -755,9 +943,11 @@ static bool replay_trace(Device &d, States *s);
 static void flush(States *s) {
     if (s->pending.empty()) {
         s->streamed = false;
+        if (s->lazy != States::kDense) materialize(dev(), s);
         return;
     }
     Device &d = dev();
+    prepare_write(d, s);
     if (replay_trace(d, s)) return;
     s->streamed = false;
     const int n = s->n_lanes;
@@ -1277,7 +1467,7 @@ int qg_qubit_states_delete(qg_handle h) {
     QG_BEGIN
     States *s = get_states(h);
     s->pending.clear();
-    if (s->d) g_dev.arena.release(s->d);
+    drop_contents(s);  // the buffer goes back to the arena unless a lazy object reads it
     g_dev.states.erase(s);
     delete s;
     QG_END
@@ -1287,8 +1477,7 @@ int qg_qubit_states_deallocate(qg_handle h) {
     QG_BEGIN
     States *s = get_states(h);
     s->pending.clear();
-    if (s->d) g_dev.arena.release(s->d);
-    s->d = nullptr;
+    drop_contents(s);
     s->n_lanes = -1;
     QG_END
 }
@@ -1339,10 +1528,13 @@ int qg_qubit_processor_initialize_qubit_states(qg_handle hp, qg_handle hs, int n
     if (n_lanes < 0 || n_lanes > 40) fail(QG_ERR_VALUE, "n_lanes %d out of range.", n_lanes);
     Device &d = dev();
     s->pending.clear();
-    if (s->d) d.arena.release(s->d);
-    s->d = nullptr;
-    s->d = d.arena.alloc(((size_t)1 << n_lanes) * complex_size(s->prec));
+    const size_t bytes = ((size_t)1 << n_lanes) * complex_size(s->prec);
+    if (d.arena.limit >= 0 && (long long)Arena::size_class(bytes) > d.arena.limit)
+        fail(QG_ERR_NOMEM, "Out of device memory. (arena limit %lld bytes, requested %zu)",
+             d.arena.limit, bytes);
+    // |0...0> without a buffer: allocated when first read or written
     s->n_lanes = n_lanes;
+    set_basis(s, 0);
     QG_END
 }
 
@@ -1350,9 +1542,15 @@ int qg_qubit_processor_reset_qubit_states(qg_handle hp, qg_handle hs) {
     QG_BEGIN
     lookup(g_dev.procs, hp, "processor");
     States *s = get_alloc_states(hs);
-    Device &d = dev();
     s->pending.clear();
-    timed(d, "init", [&] { launch_init_basis(s->prec, s->d, (idx_t)1 << s->n_lanes, d.stream); });
+    if (s->buf && s->buf.use_count() == 1) {
+        // keep the buffer (the common reset of a live state): |0...0> now
+        Device &d = dev();
+        s->lazy = States::kDense;
+        timed(d, "init", [&] { launch_init_basis(s->prec, s->d, (idx_t)1 << s->n_lanes, d.stream); });
+    } else {
+        set_basis(s, 0);
+    }
     QG_END
 }
 
@@ -1379,26 +1577,55 @@ int qg_qubit_processor_join(qg_handle hp, qg_handle hs, const qg_handle *list, i
     States *dst = get_alloc_states(hs);
     Device &d = dev();
     if (n_list < 1) fail(QG_ERR_VALUE, "join needs at least one source.");
-    std::vector<const void *> srcs(n_list);
-    std::vector<int> lanes(n_list);
+    if (n_new_lanes < 0) fail(QG_ERR_VALUE, "join: negative count of new lanes.");
+    std::vector<States *> srcs(n_list);
     int total = 0;
     for (int i = 0; i < n_list; ++i) {
         States *s = get_alloc_states(list[i]);
         if (s == dst) fail(QG_ERR_VALUE, "join destination is also a source.");
         if (s->prec != dst->prec) fail(QG_ERR_VALUE, "precision mismatch.");
-        flush(s);
-        srcs[i] = s->d;
-        lanes[i] = s->n_lanes;
+        srcs[i] = s;
         total += s->n_lanes;
     }
     if (total + n_new_lanes != dst->n_lanes)
         fail(QG_ERR_VALUE, "join: %d + %d lanes != %d.", total, n_new_lanes, dst->n_lanes);
-    dst->pending.clear();
-    idx_t prod = (idx_t)1 << total;
-    timed(d, "join", [&] {
-        launch_kron(dst->prec, dst->d, prod, srcs.data(), lanes.data(), n_list, d.stream);
-        launch_fill_zero(dst->prec, dst->d, prod, (idx_t)1 << dst->n_lanes, d.stream);
-    });
+    d.g_joins += 1;
+    // The joined state is the kron product of the sources (the last source
+    // at the lowest lanes, the new lanes |0> above them all), each source's
+    // pending gates moved up by the lanes below it; nothing runs until the
+    // product is read.  The sources keep their amplitudes and gates.
+    std::vector<Factor> fs;
+    std::vector<PendingGate> moved;
+    if (n_new_lanes > 0) {
+        Factor f;
+        f.n_lanes = n_new_lanes;
+        fs.push_back(f);
+    }
+    int offset = total;
+    for (States *s : srcs) {
+        offset -= s->n_lanes;
+        if (s->lazy == States::kView) materialize(d, s);
+        if (s->lazy == States::kProduct) {
+            fs.insert(fs.end(), s->factors.begin(), s->factors.end());
+        } else {
+            Factor f;
+            f.buf = s->buf;
+            f.n_lanes = s->n_lanes;
+            fs.push_back(f);
+        }
+        for (const PendingGate &g : s->pending) {
+            PendingGate m = g;
+            m.target += offset;
+            for (int &c : m.controls) c += offset;
+            moved.push_back(m);
+        }
+    }
+    coalesce_factors(fs);
+    drop_contents(dst);
+    dst->lazy = States::kProduct;
+    dst->factors.swap(fs);
+    dst->pending.swap(moved);
+    dst->streamed = false;
     QG_END
 }
 
@@ -1410,6 +1637,7 @@ int qg_qubit_processor_decohere(qg_handle hp, int value, double prob, qg_handle 
     if (value != 0 && value != 1) fail(QG_ERR_VALUE, "value must be 0 or 1.");
     Device &d = dev();
     flush(s);
+    prepare_write(d, s);
     double norm = value == 0 ? 1. / std::sqrt(prob) : 1. / std::sqrt(1. - prob);
     PairIdx pi = pair_pattern({lane}, 0, 1ULL << lane);
     timed(d, "measure", [&] {
@@ -1431,22 +1659,25 @@ int qg_qubit_processor_decohere_and_separate(qg_handle hp, int value, double pro
     if (s0->n_lanes != s->n_lanes - 1 || s1->n_lanes != 1)
         fail(QG_ERR_VALUE, "decohere_and_separate: wrong destination sizes.");
     if (s0->prec != s->prec || s1->prec != s->prec) fail(QG_ERR_VALUE, "precision mismatch.");
+    if (s0 == s || s1 == s || s0 == s1)
+        fail(QG_ERR_VALUE, "decohere_and_separate: the three states objects must differ.");
     Device &d = dev();
     flush(s);
+    d.g_separates += 1;
+    const double norm = value == 0 ? 1. / std::sqrt(prob) : 1. / std::sqrt(1. - prob);
+    // qstates0: a view of the source's buffer with the lane removed (formed
+    // when read: in place if the source is gone by then); qstates1 = |value>
     s0->pending.clear();
+    s0->streamed = false;
+    drop_contents(s0);
+    s0->lazy = States::kView;
+    s0->parent = s->buf;
+    s0->sep_lane = lane;
+    s0->sep_value = value;
+    s0->sep_norm = norm;
     s1->pending.clear();
-    double norm = value == 0 ? 1. / std::sqrt(prob) : 1. / std::sqrt(1. - prob);
-    PairIdx pi = pair_pattern({lane}, (unsigned long long)value << lane, 0);
-    timed(d, "measure", [&] {
-        launch_shrink(s->prec, s0->d, s->d, (idx_t)1 << (s->n_lanes - 1), pi, norm, d.stream);
-    });
-    // qstates1 = |value>
-    launch_init_basis(s1->prec, s1->d, 2, d.stream);
-    if (value == 1) {
-        PairIdx p1 = pair_pattern({0}, 0, 1);
-        Mat2 x = {{0., 0., 1., 0., 1., 0., 0., 0.}};
-        launch_apply_pairs(s1->prec, s1->d, 1, p1, x, d.stream);
-    }
+    s1->streamed = false;
+    set_basis(s1, value);
     QG_END
 }
 
@@ -1457,6 +1688,7 @@ int qg_qubit_processor_apply_reset(qg_handle hp, qg_handle hs, int lane) {
     check_lane(s, lane);
     Device &d = dev();
     flush(s);
+    prepare_write(d, s);
     PairIdx pi = pair_pattern({lane}, 0, 1ULL << lane);
     timed(d, "measure", [&] { launch_reset(s->prec, s->d, (idx_t)1 << (s->n_lanes - 1), pi, d.stream); });
     QG_END
@@ -1591,6 +1823,7 @@ int qg_circuit_run(qg_handle hc, qg_handle hs) {
         d.n_gates += (long long)c->gates.size();
     } else {
         flush(s);  // earlier gates of this states object run first
+        prepare_write(d, s);
         if (c->exec && (c->state != s->d || c->n_lanes != s->n_lanes ||
                         c->version != d.settings_version))
             drop_graph(d, c);
@@ -1651,6 +1884,7 @@ int qg_qubit_processor_apply_multi(qg_handle hp, const double *mat, qg_handle hs
     for (int i = 0; i < md.npos; ++i) md.pos[i] = pos[i];
     Device &d = dev();
     flush(s);
+    prepare_write(d, s);
     size_t dim = (size_t)1 << n_targets;
     size_t bytes = dim * dim * 2 * sizeof(double);
     void *dmat = d.arena.alloc(bytes);
@@ -1790,6 +2024,17 @@ int qg_gate_stats(int64_t *gates, int64_t *passes, int64_t *bytes, int reset) {
     QG_END
 }
 
+int qg_grouping_stats(int64_t *out, int n, int reset) {
+    QG_BEGIN
+    const long long v[7] = {g_dev.g_joins,     g_dev.g_krons,   g_dev.g_allocs, g_dev.g_separates,
+                            g_dev.g_inplace, g_dev.g_copies, g_dev.g_cow};
+    for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
+    if (reset)
+        g_dev.g_joins = g_dev.g_krons = g_dev.g_allocs = g_dev.g_separates = g_dev.g_inplace =
+            g_dev.g_copies = g_dev.g_cow = 0;
+    QG_END
+}
+
 int qg_qubit_states_get_raw(qg_handle hs, void *host, int64_t n) {
     QG_BEGIN
     States *s = get_alloc_states(hs);
@@ -1813,6 +2058,11 @@ int qg_qubit_states_set_raw(qg_handle hs, const void *host, int64_t n) {
     if (n != ((int64_t)1 << s->n_lanes)) fail(QG_ERR_VALUE, "size mismatch.");
     Device &d = dev();
     s->pending.clear();
+    if (s->lazy != States::kDense || !s->buf || s->buf.use_count() > 1) {
+        // overwritten whole: a buffer of its own, nothing to copy
+        drop_contents(s);
+        set_buffer(s, new_buffer(d, s->prec, s->n_lanes));
+    }
     QG_CUDA(cudaMemcpyAsync(s->d, host, n * complex_size(s->prec), cudaMemcpyHostToDevice,
                             d.stream));
     QG_CUDA(cudaStreamSynchronize(d.stream));

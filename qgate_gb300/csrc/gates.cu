@@ -228,12 +228,24 @@ struct KronDesc {
     const void *src[kMaxGetterStates];
     int shift[kMaxGetterStates];
     long long mask[kMaxGetterStates];
+    long long basis[kMaxGetterStates];  // src == nullptr: the basis state |basis>
 };
+
+template <class C>
+__device__ __forceinline__ C kron_factor(const KronDesc &kd, int g, idx_t d) {
+    const idx_t i = (d >> kd.shift[g]) & kd.mask[g];
+    if (kd.src[g]) return ((const C *)kd.src[g])[i];
+    C v;
+    v.x = i == kd.basis[g] ? 1 : 0;
+    v.y = 0;
+    return v;
+}
 
 // dst[d] = src[0][f0(d)] * ... * src[n-1][f_{n-1}(d)], the last source in the
 // lowest bits (np.kron order, qgate/simulator/pyruntime.py:82-97).  The
 // product is formed from the last source backwards, the order of the
 // reference's pairwise kron (qgate/simulator/src/CPUQubitProcessor.cpp:166-205).
+// A source without a buffer is a basis state (exact 0 / 1 factors).
 template <class R>
 __global__ void __launch_bounds__(kThreads)
 k_kron(typename CT<R>::type *__restrict__ dst, idx_t n_dst, KronDesc kd) {
@@ -244,13 +256,46 @@ k_kron(typename CT<R>::type *__restrict__ dst, idx_t n_dst, KronDesc kd) {
         idx_t d = base + (idx_t)u * kThreads;
         if (d < n_dst) {
             int g = kd.n_src - 1;
-            C v = ((const C *)kd.src[g])[(d >> kd.shift[g]) & kd.mask[g]];
-            for (g = kd.n_src - 2; g >= 0; --g) {
-                C w = ((const C *)kd.src[g])[(d >> kd.shift[g]) & kd.mask[g]];
-                v = cmul(w, v);
-            }
+            C v = kron_factor<C>(kd, g, d);
+            for (g = kd.n_src - 2; g >= 0; --g) v = cmul(kron_factor<C>(kd, g, d), v);
             dst[d] = v;
         }
+    }
+}
+
+// In-place removal of lane L at value v (decohere and separate): element k of
+// the (n-1)-lane result is norm * s[k with bit v inserted at L].  In chunks
+// of 2^L amplitudes, result chunk h comes from source chunk 2h + v >= h.
+// Round 0 moves chunk v to chunk 0; round j >= 1 fills chunks
+// [2^(j-1), 2^j) from chunks [2^j, 2^(j+1)): within a round sources and
+// destinations are disjoint, a destination chunk was last read as a source
+// in an earlier round, and no source chunk has been written yet.
+template <class R>
+__global__ void __launch_bounds__(kThreads)
+k_shrink_round(typename CT<R>::type *s, int L, int v, idx_t h0, idx_t h1, R norm) {
+    const idx_t n = (h1 - h0) << L;
+    const idx_t lo_mask = ((idx_t)1 << L) - 1;
+    for (idx_t k = (idx_t)blockIdx.x * kThreads + threadIdx.x; k < n;
+         k += (idx_t)gridDim.x * kThreads) {
+        const idx_t h = h0 + (k >> L), lo = k & lo_mask;
+        s[(h << L) | lo] = cscale(s[(((h << 1) | (idx_t)v) << L) | lo], norm);
+    }
+}
+
+// Rounds 0..j_last in one CTA (the first rounds are tiny), a barrier between
+// rounds.
+template <class R>
+__global__ void __launch_bounds__(1024)
+k_shrink_rounds_cta(typename CT<R>::type *s, int L, int v, int j_last, R norm) {
+    const idx_t lo_mask = ((idx_t)1 << L) - 1;
+    for (int j = 0; j <= j_last; ++j) {
+        const idx_t h0 = j ? (idx_t)1 << (j - 1) : 0, h1 = (idx_t)1 << j;
+        const idx_t n = (h1 - h0) << L;
+        for (idx_t k = threadIdx.x; k < n; k += blockDim.x) {
+            const idx_t h = h0 + (k >> L), lo = k & lo_mask;
+            s[(h << L) | lo] = cscale(s[(((h << 1) | (idx_t)v) << L) | lo], norm);
+        }
+        __syncthreads();
     }
 }
 
@@ -380,7 +425,7 @@ void launch_shrink(int prec, void *dst, const void *src, idx_t n_items, const Pa
 }
 
 void launch_kron(int prec, void *dst, idx_t n_dst, const void *const *srcs, const int *src_lanes,
-                 int n_src, cudaStream_t stream) {
+                 int n_src, cudaStream_t stream, const long long *basis) {
     if (n_src > kMaxGetterStates) fail(2, "too many states to join (%d).", n_src);
     KronDesc kd;
     kd.n_src = n_src;
@@ -389,6 +434,8 @@ void launch_kron(int prec, void *dst, idx_t n_dst, const void *const *srcs, cons
         kd.src[g] = srcs[g];
         kd.shift[g] = shift;
         kd.mask[g] = (1LL << src_lanes[g]) - 1;
+        kd.basis[g] = basis ? basis[g] : 0;
+        if (!srcs[g] && !basis) fail(2, "join source without amplitudes.");
         shift += src_lanes[g];
     }
     const int per_block = kThreads * kILP;
@@ -397,6 +444,36 @@ void launch_kron(int prec, void *dst, idx_t n_dst, const void *const *srcs, cons
     else
         k_kron<double><<<grid_for(n_dst, per_block), kThreads, 0, stream>>>((double2 *)dst, n_dst,
                                                                             kd);
+    QG_CUDA(cudaGetLastError());
+}
+
+void launch_shrink_inplace(int prec, void *state, int n_lanes, int lane, int value, double norm,
+                           cudaStream_t stream) {
+    if (lane < 0 || lane >= n_lanes || (value != 0 && value != 1))
+        fail(2, "in-place shrink: bad lane or value.");
+    const int L = lane, J = n_lanes - 1 - lane;  // rounds 0..J
+    // rounds whose cumulative size stays within 2^16 amplitudes run in one CTA
+    int j_small = -1;
+    while (j_small < J && j_small + 1 + L <= 16) ++j_small;
+    if (j_small >= 0) {
+        if (prec == kFP32)
+            k_shrink_rounds_cta<float><<<1, 1024, 0, stream>>>((float2 *)state, L, value, j_small,
+                                                               (float)norm);
+        else
+            k_shrink_rounds_cta<double><<<1, 1024, 0, stream>>>((double2 *)state, L, value,
+                                                                j_small, norm);
+    }
+    for (int j = j_small + 1; j <= J; ++j) {
+        const idx_t h0 = j ? (idx_t)1 << (j - 1) : 0, h1 = (idx_t)1 << j;
+        const idx_t n = (h1 - h0) << L;
+        const unsigned grid = grid_for(n, kThreads);
+        if (prec == kFP32)
+            k_shrink_round<float><<<grid, kThreads, 0, stream>>>((float2 *)state, L, value, h0, h1,
+                                                                 (float)norm);
+        else
+            k_shrink_round<double><<<grid, kThreads, 0, stream>>>((double2 *)state, L, value, h0,
+                                                                  h1, norm);
+    }
     QG_CUDA(cudaGetLastError());
 }
 

@@ -352,8 +352,14 @@ void launch_decohere(int prec, void *state, idx_t n_items, const PairIdx &pi, in
 void launch_reset(int prec, void *state, idx_t n_items, const PairIdx &pi, cudaStream_t stream);
 void launch_shrink(int prec, void *dst, const void *src, idx_t n_items, const PairIdx &pi,
                    double norm, cudaStream_t stream);
+// srcs[g] == nullptr with basis != nullptr: source g is the basis state
+// |basis[g]> (no buffer).
 void launch_kron(int prec, void *dst, idx_t n_dst, const void *const *srcs, const int *src_lanes,
-                 int n_src, cudaStream_t stream);
+                 int n_src, cudaStream_t stream, const long long *basis = nullptr);
+// Decohere-and-separate in place: the first 2^(n_lanes-1) amplitudes of
+// `state` become norm * (the amplitudes with lane `lane` = value), in order.
+void launch_shrink_inplace(int prec, void *state, int n_lanes, int lane, int value, double norm,
+                           cudaStream_t stream);
 void launch_apply_multi(int prec, void *state, idx_t n_items, const MultiDesc &d,
                         const void *d_mat, cudaStream_t stream);
 void launch_stage(int prec, void *state, const StageDesc &d, cudaStream_t stream);

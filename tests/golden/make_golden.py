@@ -123,6 +123,11 @@ class RecStates:
     def __init__(self, inner, sid, processor):
         self.inner, self.sid, self.processor = inner, sid, processor
 
+    def __del__(self):
+        # the front-end dropped its last reference (after a join or a
+        # separation, qgate/simulator/qubits_handler.py:67-68, :100)
+        self.processor.log.calls.append(['delete_states', self.sid])
+
     def get_n_lanes(self):
         return self.inner.get_n_lanes()
 
@@ -283,6 +288,27 @@ def scenarios(qgate):
         pool.sample(5000, np.random.default_rng(seed + 1).random(5000))
         return sim
     out['random_u3cx_10'] = lambda: s_random(10, 5, 10)
+
+    def s_random_dynamic(n, depth, seed):
+        """The random U3 + CX circuit under the default dynamic qubit
+        grouping: every qubit starts in its own states object, CX gates join
+        groups, and measuring every qubit separates them again."""
+        rng = np.random.default_rng(seed)
+        q = new_qregs(n)
+        r = new_references(n)
+        c = []
+        for _ in range(depth):
+            ang = rng.uniform(0, 2 * math.pi, (n, 3))
+            c += [U3(*ang[i])(q[i]) for i in range(n)]
+            perm = rng.permutation(n)
+            c += [ctrl(q[perm[2 * k]]).X(q[perm[2 * k + 1]]) for k in range(n // 2)]
+        c += [prob(r[i], q[i]) for i in range(n)]
+        c += [measure(r[i], q[i]) for i in rng.permutation(n)]
+        sim = qgate.simulator.cpu(circuit_prep=qgate.prefs.dynamic)
+        sim.run(c)
+        dump_all(sim, q)
+        return sim
+    out['random_u3cx_12_dynamic'] = lambda: s_random_dynamic(12, 4, 12)
     out['random_u3cx_13'] = lambda: s_random(13, 4, 11)
 
     def s_gateset():

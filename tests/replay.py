@@ -90,6 +90,13 @@ def replay(calls, arrays, runtime, dtype):
         if op == 'new_states':
             objs[c[1]] = runtime.create_qubit_states(dtype)
             last_qs = objs[c[1]]
+        elif op == 'delete_states':
+            qs = objs.pop(c[1], None)
+            if qs is not None:
+                if qs is last_qs:
+                    last_qs = None
+                if hasattr(qs, 'delete'):
+                    qs.delete()
         elif op == 'new_getter':
             getter = objs[c[1]] = runtime.create_qubits_states_getter(dtype)
         elif op == 'init':
