@@ -253,8 +253,11 @@ def run_reference(args):
             st.apply(m, t, c)
     dt = time.perf_counter() - t0
     value = step_bytes * args.steps / dt / 1e9
-    sample_desc = ('first %d gates of the circuit per step on a 2^%d %s state in host memory'
-                   % (len(sample), n, args.dtype))
+    n_cx = sum(1 for _, _, _, c in sample if c)
+    sample_desc = ('first %d gates of the circuit (%d U3 + %d CX) per step on a 2^%d %s state '
+                   'in host memory; the port runs at the reference CPU runtime\'s own rate '
+                   '(oracle/port_speed.py: 0.99x with 8 threads, 1.33x on one thread, x86 '
+                   'build host)' % (len(sample), len(sample) - n_cx, n_cx, n, args.dtype))
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'GB/s',
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
@@ -875,7 +878,9 @@ def main():
     ap.add_argument('--adj-batch', type=int, default=64)
     ap.add_argument('--adj-steps', type=int, default=1)
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
-    ap.add_argument('--ref-gates', type=int, default=12)
+    # the reference arm's step: the circuit's first layer at 30 qubits (30 U3
+    # + 15 CX), the same gate mix as the whole circuit
+    ap.add_argument('--ref-gates', type=int, default=45)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == 'gb300':
         print('note: fewer than 3 warm-up steps', file=sys.stderr)
