@@ -309,6 +309,9 @@ def run_gb300(args):
     else:
         nat.set_fusion(args.tile)
         tuned = {'tile_lanes': args.tile}
+    if args.no_tensor:
+        nat.set_tensor_blocks(False)
+        tuned = dict(tuned, tensor=0)
 
     qs = rt.create_qubit_states(dtype)
     proc = qs.processor
@@ -323,6 +326,10 @@ def run_gb300(args):
                 proc.apply_gate(gt, False, qs, t)
         proc.synchronize()
 
+    # Trace replay off for the timed circuit: every stage is its own timed
+    # launch (with tensor stages the 900-gate circuit streams anyway, which
+    # trace replay leaves alone; with --no-tensor it would replay one graph)
+    nat.set_trace_replay(False)
     for _ in range(args.warmup):
         step()
     stream = torch.cuda.ExternalStream(nat.stream_handle())
@@ -340,6 +347,7 @@ def run_gb300(args):
     e1.record(stream)
     torch.cuda.synchronize()
     nat.timing_enable(False)
+    nat.set_trace_replay(True)
     clocks = sampler.stop()
     dev_ms = e0.elapsed_time(e1)
     stats = nat.gate_stats(reset=True)
@@ -859,6 +867,8 @@ def main():
     ap.add_argument('--tile', type=int, default=0,
                     help='fusion tile lanes (0 = autotuned, 1 = fusion off)')
     ap.add_argument('--retune', action='store_true', help='ignore the autotuner cache')
+    ap.add_argument('--no-tensor', action='store_true',
+                    help='complex64 stages on the CUDA cores (k_rstage) instead of tcgen05 blocks')
     ap.add_argument('--samples', type=int, default=10_000_000)
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-e2e', action='store_true')
