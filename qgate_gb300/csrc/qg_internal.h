@@ -157,6 +157,13 @@ struct TcStageDesc {
     int ins_pos[kMaxTileLanes];
     long long dep_hi[32];
     long long in_e[5];                    // dep_hi[1 << k]
+    // direct_out = 1: the final layout's warp rows hold tile positions 0..3
+    // (whole 128-byte lines), so rows are stored straight to the state:
+    // row bit b at global lane out_row_lane[b], amplitude bit k at out_e[k].
+    // Otherwise rows go through the natural tile (sets[nb], sets[nb + 1]).
+    int direct_out;
+    int out_row_lane[8];
+    long long out_e[5];
     int nblocks;                          // ops
     unsigned ops_bytes;
     unsigned op_off[kMaxTcBlocks];        // byte offset of op b's operands

@@ -428,6 +428,37 @@ static unsigned tc_fill_lanes(unsigned lanes, const TcLayout &src, int m) {
     return lanes;
 }
 
+// Tile positions 0..3 (global lanes 0..3: the sixteen amplitudes of a
+// 128-byte line) on a warp's row bits make its row stores two whole lines
+// per instruction, as the load layout's loads are.  (Positions 0 and 1 alone,
+// eight whole 32-byte sectors per instruction, measured slower than the trip
+// through the natural tile.)
+constexpr unsigned kDirectLow = 15u;
+
+// tc_fill_lanes that never adds the positions in `avoid`.
+static unsigned tc_fill_lanes_avoiding(unsigned lanes, const TcLayout &src, int m,
+                                       unsigned avoid) {
+    for (int x = 0; x < 5 && __builtin_popcount(lanes) < 5; ++x) {
+        unsigned in_warp = 0;
+        for (int y = 0; y < 5; ++y) in_warp += lanes >> src.rows[y] & 1u;
+        if (in_warp >= 2) break;
+        if (avoid >> src.rows[x] & 1u) continue;
+        lanes |= 1u << src.rows[x];
+    }
+    for (int p = 0; p < m && __builtin_popcount(lanes) < 5; ++p)
+        if (!(avoid >> p & 1u)) lanes |= 1u << p;
+    return lanes;
+}
+
+// Moves tile position p to rows[x] (swapping with whatever was there).
+static void tc_place_row(TcLayout &c, int p, int x) {
+    for (int i = 0; i < 8; ++i)
+        if (c.rows[i] == p) {
+            std::swap(c.rows[i], c.rows[x]);
+            return;
+        }
+}
+
 // Shared-memory wavefronts of one warp-wide 4-byte store through slot
 // tables: the largest number of threads on one bank.
 static int tc_store_cost(const SetSlots &ss) {
@@ -521,8 +552,37 @@ static void tc_phase_table(const TcOp &op, const TileLanes &tl, const std::vecto
 // Host plan of one tensor-stage launch: ops [b0, b0 + nb) of a stage on tile
 // `tl` -> the descriptor (all but the operand pointer) and the ops' operands
 // in `buf`.
+static void tc_plan_launch_ordered(const TileLanes &tl, int n, const TcOps &ops, size_t b0,
+                                   int nb, TcStageDesc &desc, unsigned char *buf);
+
 void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int nb,
                     TcStageDesc &desc, unsigned char *buf) {
+    // The launch's ops in an order that ends with a dense op leaving tile
+    // positions 0..3 to the rows (its rows then go straight to the state):
+    // a dense op moves to the end when it shares no lane with any op after
+    // it (disjoint ops commute), the latest such op first.
+    TcOps slice(ops.begin() + b0, ops.begin() + b0 + nb);
+    int last = -1;
+    for (int b = nb - 1; b >= 0 && last < 0; --b)
+        if (!slice[b].phase) last = b;
+    if (last >= 0 && (slice[last].lanes & kDirectLow)) {
+        for (int x = last - 1; x >= 0; --x) {
+            if (slice[x].phase || (slice[x].lanes & kDirectLow)) continue;
+            bool disjoint = true;
+            for (int y = x + 1; y < nb && disjoint; ++y) disjoint = !(slice[y].lanes & slice[x].lanes);
+            if (disjoint) {
+                TcOp mv = slice[x];
+                slice.erase(slice.begin() + x);
+                slice.push_back(mv);
+                break;
+            }
+        }
+    }
+    tc_plan_launch_ordered(tl, n, slice, 0, nb, desc, buf);
+}
+
+static void tc_plan_launch_ordered(const TileLanes &tl, int n, const TcOps &ops, size_t b0,
+                                   int nb, TcStageDesc &desc, unsigned char *buf) {
     const int m = (int)tl.lanes.size();
     const int t = m - 5;
     memset(&desc, 0, sizeof(desc));
@@ -583,6 +643,8 @@ void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int
             }
         }
     }
+    // phase-only launches end in the load layout (coalesced by construction)
+    bool direct_out = last_dense < 0;
     for (int b = 0; b < t; ++b) desc.row_lane[b] = tl.lanes[cur.rows[b]];
     for (int j = 0; j < 32; ++j) {
         long long off = 0;
@@ -614,11 +676,42 @@ void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int
             tc_phase_table(op, tl, order, (float *)(buf + desc.op_off[b]));
             continue;
         }
-        unsigned lanes = tc_fill_lanes(op.lanes, cur, m);
+        // The last dense op stores its rows straight to the state when its
+        // block leaves tile positions 0..3 (the low lanes of a 128-byte line)
+        // to the rows: those four then go among the warp's row bits.
+        const unsigned low = b == last_dense && !(op.lanes & kDirectLow) ? kDirectLow : 0u;
+        const bool direct = low != 0u;
+        unsigned lanes = direct ? tc_fill_lanes_avoiding(op.lanes, cur, m, low)
+                                : tc_fill_lanes(op.lanes, cur, m);
         const int nd = next_dense(b);
         const unsigned next = nd >= 0 ? ops[b0 + nd].lanes : 0u;
         TcLayout lay = tc_choose_layout(lanes, next, cur, m);
-        if (b == last_dense) {
+        if (direct) {
+            // positions 0..3 into rows[0..4], in every choice of slots and
+            // order, where the operand stores of this op hit the fewest banks
+            // twice
+            const int np = __builtin_popcount(low);
+            int best = 1 << 30;
+            const TcLayout keep = lay;
+            for (unsigned mask = 0; mask < 32u; ++mask) {
+                if (__builtin_popcount(mask) != np) continue;
+                int slots[4], k = 0;
+                for (int x = 0; x < 5; ++x)
+                    if (mask >> x & 1u) slots[k++] = x;
+                int perm[4] = {0, 1, 2, 3};
+                do {
+                    TcLayout c = keep;
+                    for (int i = 0; i < np; ++i) tc_place_row(c, perm[i], slots[i]);
+                    const int cost = tc_store_cost(
+                        tc_slots(cur, t, [&](unsigned ti) { return tc_operand_slot(c, ti); }));
+                    if (cost < best) {
+                        best = cost;
+                        lay = c;
+                    }
+                } while (std::next_permutation(perm, perm + np));
+            }
+            direct_out = true;
+        } else if (b == last_dense) {
             // Last dense op: rows[3..4] only feed the 8-byte stores into the
             // natural tile; pick them for the fewest wavefronts there.
             int best = 1 << 30;
@@ -646,6 +739,9 @@ void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int
         cur = lay;
     }
     desc.sets[nb] = tc_slots(cur, t, [&](unsigned ti) { return host_swz(ti, kFP32); });
+    desc.direct_out = direct_out ? 1 : 0;
+    for (int b = 0; b < 8; ++b) desc.out_row_lane[b] = b < t ? tl.lanes[cur.rows[b]] : 0;
+    for (int k = 0; k < 5; ++k) desc.out_e[k] = 1LL << tl.lanes[cur.amps[k]];
 }
 
 

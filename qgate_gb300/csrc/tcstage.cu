@@ -382,6 +382,22 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tile
         tc_fence_before();
         group_sync(gbar, TG);  // every thread's products read: the buffers are free
         if (!ok) break;
+        if (d.direct_out) {
+            // The final layout's warp rows cover whole 128-byte lines: rows
+            // go straight from the registers to the state, then the next
+            // tile's loads.
+            idx_t o = 0;
+            for (int b = 0; b < t; ++b)
+                if (r & (1u << b)) o |= 1LL << d.out_row_lane[b];
+            if (H == 2 && hh) o += d.out_e[4];
+            float2 *gp = s + (insert_zeros((idx_t)tl, d.ins_pos, d.nins) | o);
+            gray_walk<NB>(gp, d.out_e, [&](int j, float2 *p) {
+                *p = make_float2(__uint_as_float(v[2 * j]) * kUnscale,
+                                 __uint_as_float(v[2 * j + 1]) * kUnscale);
+            });
+            if (tl + tstep < tiles) load_raw(tl + tstep);
+            continue;
+        }
         // Last layout -> swizzled natural tile -> load layout -> global.
         {
             const SetSlots &ss = sset[nb];

@@ -184,7 +184,7 @@ int main(int argc, char **argv) {
             for (unsigned ti = 0; ti < 4096; ++ti) seen.insert(tc_operand_slot(L, ti));
             if (seen.size() != 4096 || *seen.rbegin() >= 4096) ++bad_slots;
         }
-        int bad_tables = 0, launches = 0, phase_ops = 0, dense_ops = 0;
+        int bad_tables = 0, launches = 0, phase_ops = 0, dense_ops = 0, direct_launches = 0;
         double worst_emul = 0.;
         auto b_index = [](int k, int nn) {  // the FP16 index of B[k][n] in Bh (Bl: + 4096)
             return (size_t)(k / 16) * 1024 + (k % 16 / 8) * 512 + (nn / 8) * 64 + (nn % 8) * 8 + k % 8;
@@ -286,14 +286,40 @@ int main(int argc, char **argv) {
                     }
                 }
             }
-            // copy-out: final layout -> natural tile -> load layout
-            std::vector<cd> nat((size_t)1 << m);
-            for (unsigned r = 0; r < (unsigned)TR; ++r)
-                for (unsigned j = 0; j < 32; ++j) nat[slot_of(desc.sets[nb], r, j)] = V[r][j];
+            // copy-out: final layout -> natural tile -> load layout, or
+            // (direct_out) final layout straight to the state's offsets
             std::map<long long, cd> got;
-            for (unsigned r = 0; r < (unsigned)TR; ++r)
-                for (unsigned j = 0; j < 32; ++j)
-                    got[load_off(r, j)] = nat[slot_of(desc.sets[nb + 1], r, j)];
+            if (desc.direct_out) {
+                ++direct_launches;
+                std::map<long long, int> hit;
+                for (unsigned r = 0; r < (unsigned)TR; ++r) {
+                    long long ro = 0;
+                    for (int b = 0; b < t; ++b)
+                        if (r >> b & 1u) ro |= 1LL << desc.out_row_lane[b];
+                    // a warp's rows cover whole 128-byte lines (lanes 0..3)
+                    for (unsigned j = 0; j < 32; ++j) {
+                        long long off = ro;
+                        for (int k = 0; k < 5; ++k)
+                            if (j >> k & 1u) off |= desc.out_e[k];
+                        got[off] = V[r][j];
+                        hit[off] += 1;
+                    }
+                }
+                // every amplitude of the tile written once
+                if (hit.size() != want.size()) ++bad_tables;
+                for (auto &kv : hit)
+                    if (kv.second != 1 || !want.count(kv.first)) ++bad_tables;
+                unsigned wl = 0;
+                for (int b = 0; b < 5; ++b) wl |= 1u << desc.out_row_lane[b];
+                if ((wl & 15u) != 15u) ++bad_tables;
+            } else {
+                std::vector<cd> nat((size_t)1 << m);
+                for (unsigned r = 0; r < (unsigned)TR; ++r)
+                    for (unsigned j = 0; j < 32; ++j) nat[slot_of(desc.sets[nb], r, j)] = V[r][j];
+                for (unsigned r = 0; r < (unsigned)TR; ++r)
+                    for (unsigned j = 0; j < 32; ++j)
+                        got[load_off(r, j)] = nat[slot_of(desc.sets[nb + 1], r, j)];
+            }
             for (int b = 0; b < nb; ++b)
                 for (auto *g : ops[b].gates) {
                     const long long tb = 1LL << g->target;
@@ -316,7 +342,8 @@ int main(int argc, char **argv) {
         }
         printf("emulated_stage_max_rel_err %.3e\nphase_ops %d\ndense_ops %d\n", worst_emul,
                phase_ops, dense_ops);
-        printf("bad_slots %d\nbad_tables %d\nlaunches_checked %d\n", bad_slots, bad_tables, launches);
+        printf("bad_slots %d\nbad_tables %d\nlaunches_checked %d\ndirect_out_launches %d\n",
+               bad_slots, bad_tables, launches, direct_launches);
     }
     return 0;
 }

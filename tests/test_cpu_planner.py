@@ -69,10 +69,15 @@ def test_operand_slot_tables_are_bijections(planner_run):
 
 def test_emulated_stage_matches_the_gates(planner_run):
     """The tensor-stage kernel's data flow emulated in FP64 from launch plans
-    (load layout, slot tables, Bh + Bl operands or phase tables, natural tile)
+    (load layout, slot tables, Bh + Bl operands or phase tables, natural tile
+    or the direct row stores)
     equals the plans' gates applied to the tile, for 12- and 13-lane tiles
     with dense and phase ops; what remains is the operands' FP16 split (~2^-22
     per op) and the compensation scale (~1e-7 per dense op)."""
     vals, _ = planner_run
     assert float(vals['emulated_stage_max_rel_err']) < 5e-6
     assert int(vals['phase_ops']) > 0 and int(vals['dense_ops']) > 0
+    # launches that store rows straight to the state (their last dense block
+    # leaves lanes 0 and 1 to the rows) and ones through the natural tile
+    direct = int(vals['direct_out_launches'])
+    assert 0 < direct < int(vals['launches_checked'])
