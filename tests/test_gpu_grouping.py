@@ -203,3 +203,60 @@ def test_separate_then_gates_and_rejoin(rt, dtype):
     assert np.allclose(joined.get_raw(), want, atol=4 * ATOL[dtype])
     for x in (qs0, qs1, joined):
         x.delete()
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_lazy_products_read_by_getter_pool_and_compiled_runs(rt, dtype):
+    """Joined objects that were never read (products of buffers and |0>
+    factors with gates pending) go straight into a gather with swapped lanes,
+    a sampling pool and a compiled-circuit run; each matches the oracle."""
+    from qgate_gb300.circuit import Lane, abs2, gate_type
+    from qgate_gb300.compiled import CompiledCircuit
+    rng = np.random.default_rng(45)
+    parts, psis = [], []
+    for k in (3, 2, 4):
+        qs = new_state(rt, k, dtype)
+        ops = random_ops(rng, k, 12)
+        apply_ops(qs, ops)
+        parts.append(qs)
+        psis.append(sv.run_ops(k, ops))
+    parts[0].processor.synchronize()  # the first part formed, the others not
+    a = rt.create_qubit_states(dtype)
+    a.processor.initialize_qubit_states(a, 5)
+    a.processor.join(a, [parts[0], parts[1]], 0)
+    b = rt.create_qubit_states(dtype)
+    b.processor.initialize_qubit_states(b, 6)
+    b.processor.join(b, [parts[2]], 2)
+    psi_a = sv.join([psis[0], psis[1]], 0)
+    psi_b = sv.join([psis[2]], 2)
+    # gather: lanes of a and b interleaved in the external order
+    la = [Lane(l, e) for l, e in zip(range(5), (0, 2, 4, 6, 8))]
+    lb = [Lane(l, e) for l, e in zip(range(6), (1, 3, 5, 7, 9, 10))]
+    getter = rt.create_qubits_states_getter(dtype)
+    probs = np.empty(1 << 11, dtype)
+    getter.get_states(probs, 0, abs2, [(a, la), (b, lb)], [], 1 << 11, 0, 1)
+    pa, pb = np.abs(psi_a) ** 2, np.abs(psi_b) ** 2
+    want = np.zeros(1 << 11)
+    for x in range(1 << 11):
+        ia = sum(((x >> e) & 1) << l for l, e in zip(range(5), (0, 2, 4, 6, 8)))
+        ib = sum(((x >> e) & 1) << l for l, e in zip(range(6), (1, 3, 5, 7, 9, 10)))
+        want[x] = pa[ia] * pb[ib]
+    assert np.allclose(probs, want, atol=4 * ATOL[dtype])
+    # a pool over b alone, then a compiled run on a fresh lazy product
+    pool = getter.create_sampling_pool(list(range(6)), 6, 0, [(b, [Lane(l, l) for l in range(6)])],
+                                       [])
+    u = rng.random(2000)
+    obs = np.asarray(pool.sample(len(u), u).intarray)
+    assert np.mean(obs == sv.SamplingPool(pb).sample(u)) > 0.99
+    pool.delete()
+    c = rt.create_qubit_states(dtype)
+    c.processor.initialize_qubit_states(c, 7)
+    c.processor.join(c, [parts[1]], 5)
+    cops = random_ops(rng, 7, 16, max_controls=1)
+    circ = CompiledCircuit(dtype, [(gate_type(nm, *args), adj, t, list(cs))
+                                   for _, nm, args, adj, t, cs in cops], graph=True)
+    circ.run(c)
+    want_c = sv.run_ops(7, cops, psi=sv.join([psis[1]], 5))
+    assert np.allclose(c.get_raw(), want_c, atol=4 * ATOL[dtype])
+    for x in parts + [a, b, c]:
+        x.delete()
