@@ -2264,6 +2264,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                     fill_tile_header(tl, n, 4, sp.hdr.lowrun, sp.hdr.nhi, sp.hdr.hi_pos,
                                      sp.hdr.nins, sp.hdr.ins_pos, sp.hdr.dep_hi);
                     sp.hdr.nops = (int)prog.size();
+                    sp.hdr.nsets = (int)sets.size();
                     sp.hdr.ops_off = (long long)P.ops.size();
                     sp.hdr.sets_off = (int)P.sets.size();
                     sp.live = 0;

@@ -216,8 +216,14 @@ __global__ void k_batch_init(C *arena, const long long *__restrict__ off, int co
 // ---------------------------------------------------------------- one launch
 
 constexpr unsigned kBatchThreads = 256;
-// a 12-qubit resident state, or two tiles (the one running, the next loading)
-constexpr size_t kBatchSmem = sizeof(C) << 13;
+// a 12-qubit resident state, or two tiles (the one running, the next
+// loading) and the running stage's program: its ops and register sets, read
+// by every op of every tile of an item (from global memory they would come
+// from L2 whenever the tile loads have pushed them out of L1)
+constexpr int kBatchProgOps = 192, kBatchProgSets = 64;
+constexpr size_t kBatchTileBytes = sizeof(C) << 13;
+constexpr size_t kBatchSmem = kBatchTileBytes + kBatchProgOps * sizeof(RegOp<R>) +
+                              kBatchProgSets * sizeof(SetSlots);
 constexpr long long kBatchWaitTries = 1LL << 22;  // x ~100 ns sleeps: ~0.5 s
 
 // Waits (thread 0) until counter >= need; bounded: a wait that gives up
@@ -340,6 +346,24 @@ k_batch_persistent(const BatchItem *__restrict__ items, int n_items, int *head, 
             for (int b = lr; b < t; ++b)
                 if (tid & (1u << b)) dt |= 1LL << st.hi_pos[b - st.lowrun];
             const unsigned pt = Swz<R>::f(tid);
+            // the stage's program into shared memory (when it fits)
+            const RegOp<R> *prog_ops = ops_all + st.ops_off;
+            const SetSlots *prog_sets = sets_all + st.sets_off;
+            if (st.nops <= kBatchProgOps && st.nsets <= kBatchProgSets) {
+                RegOp<R> *sops = (RegOp<R> *)(smraw + kBatchTileBytes);
+                SetSlots *ssets = (SetSlots *)(sops + kBatchProgOps);
+                const int4 *go = (const int4 *)prog_ops;
+                int4 *so = (int4 *)sops;
+                const int n16 = st.nops * (int)(sizeof(RegOp<R>) / 16);
+                for (int i = (int)tid; i < n16; i += (int)kBatchThreads) so[i] = go[i];
+                const unsigned *gs = (const unsigned *)prog_sets;
+                unsigned *ss = (unsigned *)ssets;
+                const int n4 = st.nsets * (int)(sizeof(SetSlots) / 4);
+                for (int i = (int)tid; i < n4; i += (int)kBatchThreads) ss[i] = gs[i];
+                prog_ops = sops;
+                prog_sets = ssets;
+                // made visible to every thread by the barrier before the first op
+            }
             auto load_tile = [&](C *buf, int tile) {
                 const idx_t base = insert_zeros((idx_t)tile, st.ins_pos, st.nins);
 #pragma unroll
@@ -378,8 +402,7 @@ k_batch_persistent(const BatchItem *__restrict__ items, int n_items, int *head, 
                 unsigned e0 = 0, P0 = 0, q[RL], lanebit[RL];
 #pragma unroll
                 for (int k = 0; k < RL; ++k) q[k] = lanebit[k] = 0;
-                run_program<RL>(a, cur, ops_all + st.ops_off, st.nops, sets_all + st.sets_off,
-                                tid, e0, P0, q, lanebit);
+                run_program<RL>(a, cur, prog_ops, st.nops, prog_sets, tid, e0, P0, q, lanebit);
                 __syncthreads();
 #pragma unroll
                 for (int i = 0; i < NR; ++i) cur[reg_slot<RL>(P0, q, i)] = a[i];

@@ -273,7 +273,7 @@ struct BatchStage {
     long long dep_hi[1 << kMaxRegLanes];
     long long ops_off;    // index of the stage's first RegOp in the program buffer
     int sets_off;         // index of the stage's first register set
-    int pad;
+    int nsets;            // register sets of the stage
 };
 
 // Circuits that fit one CTA: 2^n amplitudes of complex64 in shared memory,
