@@ -885,9 +885,11 @@ static void flush_lookahead(Device &d, States *s, std::vector<const PendingGate 
             remaining.erase(remaining.begin());
             continue;
         }
-        unsigned long long S = plan_stage_lanes(remaining, base, M);
+        // cross gates (diagonal gates with at most one lane in the tile) run
+        // in any stage as per-tile phases
+        unsigned long long S = plan_stage_lanes(remaining, base, M, true, kMaxTensorStageGates);
         std::vector<const PendingGate *> chosen, deferred;
-        stage_take(remaining, S, remaining.size(), &chosen, &deferred);
+        stage_take(remaining, S, remaining.size(), &chosen, &deferred, true, kMaxTensorStageGates);
         if (chosen.size() == 1) {
             run_single_gate(d, s, *chosen[0]);
         } else {

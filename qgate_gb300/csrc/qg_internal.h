@@ -150,6 +150,29 @@ template <class R> struct RStageDesc {
 // values, canonical K-major layout), a phase op's table of complex64 phases
 // (ops_bytes in all, a multiple of 16).
 constexpr int kMaxTcBlocks = 24;
+// Operands of a cross op (op_kind 2): this header, then `nrec` records
+// sorted by tile position.  Records of position p < m are [start[p],
+// start[p + 1]); records [start[m], nrec) act on no tile lane (a per-tile
+// scalar).  A record applies when the tile's amplitude index has every bit
+// of `need` set; with tgt == 0 (the gate's target is at p) it adds angle a0
+// to the phase of bit p = 0 and a1 to bit p = 1; otherwise (the target is
+// outside the tile, at the lanes of tgt) it adds (tile bit tgt ? a1 : a0) to
+// bit p = 1 (or to the scalar).  rows / amps: tile positions of the row bits
+// and register bits of the layout the op runs in.
+struct TcCrossHdr {
+    int nrec;
+    int start[15];
+    signed char rows[8];
+    signed char amps[5];
+    signed char pad[3];
+};
+struct TcCrossRec {
+    long long need, tgt;
+    float a0, a1;  // in (-pi, pi]
+    float pad[2];
+};
+static_assert(sizeof(TcCrossHdr) % 16 == 0 && sizeof(TcCrossRec) == 32, "cross op layout");
+
 struct TcStageDesc {
     int n, m;
     int row_lane[8];
@@ -167,7 +190,7 @@ struct TcStageDesc {
     int nblocks;                          // ops
     unsigned ops_bytes;
     unsigned op_off[kMaxTcBlocks];        // byte offset of op b's operands
-    unsigned char op_kind[kMaxTcBlocks];  // 0: dense block, 1: phase table
+    unsigned char op_kind[kMaxTcBlocks];  // 0: dense block, 1: phase table, 2: cross
     const unsigned char *bmats;
     SetSlots sets[kMaxTcBlocks + 2];
 };

@@ -33,13 +33,26 @@ TileLanes tile_lanes_of(unsigned long long S, int n) {
 }
 
 
+// A diagonal gate whose two entries have modulus 1 (so they are phases).
+static bool unit_diag(const PendingGate &g) {
+    if (!g.diag) return false;
+    auto unit = [](double re, double im) { return std::fabs(re * re + im * im - 1.) < 1e-12; };
+    return unit(g.m.v[0], g.m.v[1]) && unit(g.m.v[6], g.m.v[7]);
+}
+
+bool cross_gate(const PendingGate &g, unsigned long long S) {
+    const unsigned long long q = gate_qmask(g);
+    return (q & ~S) && __builtin_popcountll(q & S) <= 1 && unit_diag(g);
+}
+
 // Gates of `gates` (in order) that a stage on lane set S takes: a gate is
-// taken when its lanes lie in S and no earlier gate that was left out shares
-// a lane with it (so it commutes with everything left out before it).  At
-// most `limit` gates are scanned and kMaxStageGates taken; returns the count.
+// taken when its lanes lie in S (or, with `cross`, it is a cross gate) and
+// no earlier gate that was left out shares a lane with it (so it commutes
+// with everything left out before it).  At most `limit` gates are scanned
+// and `max_take` taken; returns the count.
 int stage_take(const std::vector<const PendingGate *> &gates, unsigned long long S,
-                      size_t limit, std::vector<const PendingGate *> *take,
-                      std::vector<const PendingGate *> *keep) {
+               size_t limit, std::vector<const PendingGate *> *take,
+               std::vector<const PendingGate *> *keep, bool cross, int max_take) {
     unsigned long long blocked = 0;
     int count = 0;
     for (size_t i = 0; i < gates.size(); ++i) {
@@ -50,7 +63,8 @@ int stage_take(const std::vector<const PendingGate *> &gates, unsigned long long
             continue;
         }
         const unsigned long long q = gate_qmask(*g);
-        if ((q & blocked) || (q & ~S) || count >= kMaxStageGates) {
+        const bool fits = !(q & ~S) || (cross && cross_gate(*g, S));
+        if ((q & blocked) || !fits || count >= max_take) {
             blocked |= q;
             if (keep) keep->push_back(g);
             continue;
@@ -62,15 +76,20 @@ int stage_take(const std::vector<const PendingGate *> &gates, unsigned long long
 }
 
 
-// stage_take's count over precomputed lane masks: the same walk, stopped
-// once every lane of S is blocked (no later gate can be taken then).
-static int take_count(const std::vector<unsigned long long> &q, unsigned long long S) {
+// stage_take's count over precomputed lane masks (xd: the gate is a
+// unit-modulus diagonal, so a cross gate wherever at most one of its lanes
+// is in S): the same walk, stopped once every lane of S is blocked (without
+// cross gates no later gate can be taken then).
+static int take_count(const std::vector<unsigned long long> &q, const std::vector<char> &xd,
+                      unsigned long long S, bool cross, int max_take) {
     unsigned long long blocked = 0;
     int count = 0;
-    for (const unsigned long long g : q) {
-        if ((g & blocked) || (g & ~S) || count >= kMaxStageGates) {
+    for (size_t i = 0; i < q.size(); ++i) {
+        const unsigned long long g = q[i];
+        const bool fits = !(g & ~S) || (cross && xd[i] && __builtin_popcountll(g & S) <= 1);
+        if ((g & blocked) || !fits || count >= max_take) {
             blocked |= g;
-            if ((blocked & S) == S) break;
+            if (!cross && (blocked & S) == S) break;
             continue;
         }
         ++count;
@@ -81,18 +100,22 @@ static int take_count(const std::vector<unsigned long long> &q, unsigned long lo
 // Lane set (M lanes, including `base` and the first gate's lanes) of the next
 // tensor-core stage over `remaining` (see flush_lookahead).
 unsigned long long plan_stage_lanes(const std::vector<const PendingGate *> &remaining,
-                                    unsigned long long base, int M) {
+                                    unsigned long long base, int M, bool cross, int max_take) {
     const size_t kWindow = 512;
     const unsigned long long q0 = gate_qmask(*remaining[0]);
     unsigned long long cand_all = 0;
     std::vector<unsigned long long> qw;
+    std::vector<char> xd;
     qw.reserve(std::min(remaining.size(), kWindow));
     for (size_t i = 0; i < remaining.size() && i < kWindow; ++i) {
         qw.push_back(gate_qmask(*remaining[i]));
+        xd.push_back(cross && unit_diag(*remaining[i]));
         cand_all |= qw.back();
     }
     auto stage_take = [&](const std::vector<const PendingGate *> &, unsigned long long S, size_t,
-                          std::nullptr_t, std::nullptr_t) { return take_count(qw, S); };
+                          std::nullptr_t, std::nullptr_t) {
+        return take_count(qw, xd, S, cross, max_take);
+    };
     const unsigned long long fixed = base | q0;
     // Greedy growth from `S0`: add the lane that lets the stage take the
     // most gates until the stage has M lanes.
@@ -311,16 +334,41 @@ static void tc_compensate(std::complex<double> *U) {
 // Greedy 5-lane blocks over a stage's gates in order: a gate joins the open
 // block when its lanes fit and no earlier deferred gate shares a lane (so it
 // commutes with everything deferred); the rest start the next block.
+// Cross gates (lanes outside the tile) never join a block; a cross gate
+// keeps the later non-diagonal gates of its tile lane out of the blocks
+// (diagonal gates commute with it).  Cross gates are left as late as
+// possible, so that few cross ops hold them all: only when no block can take
+// a gate, every cross gate that no earlier remaining non-diagonal gate shares
+// its tile lane with forms a cross block.  Without cross gates this is the
+// plain greedy walk.
 TcBlocks tc_blocks(const std::vector<const PendingGate *> &gates, const TileLanes &tl) {
     std::vector<std::pair<unsigned, std::vector<const PendingGate *>>> out;
     std::vector<const PendingGate *> rem(gates);
+    // tile-position mask of g's lanes in the tile; false if some lane is outside
+    auto tile_mask = [&](const PendingGate *g, unsigned &q) {
+        bool in = true;
+        q = 0;
+        const int pt = tl.local_of[g->target];
+        if (pt < 0) in = false;
+        else q |= 1u << pt;
+        for (int c : g->controls) {
+            const int pc = tl.local_of[c];
+            if (pc < 0) in = false;
+            else q |= 1u << pc;
+        }
+        return in;
+    };
     while (!rem.empty()) {
-        unsigned L = 0, blocked = 0;
+        unsigned L = 0, blocked = 0, blocked_nd = 0;
         std::vector<const PendingGate *> take, keep;
         for (auto *g : rem) {
-            unsigned q = 1u << tl.local_of[g->target];
-            for (int c : g->controls) q |= 1u << tl.local_of[c];
-            if ((q & blocked) || __builtin_popcount(L | q) > 5) {
+            unsigned q;
+            if (!tile_mask(g, q)) {
+                keep.push_back(g);
+                blocked_nd |= q;
+                continue;
+            }
+            if ((q & blocked) || (!g->diag && (q & blocked_nd)) || __builtin_popcount(L | q) > 5) {
                 keep.push_back(g);
                 blocked |= q;
                 continue;
@@ -328,7 +376,29 @@ TcBlocks tc_blocks(const std::vector<const PendingGate *> &gates, const TileLane
             L |= q;
             take.push_back(g);
         }
-        out.emplace_back(L, std::move(take));
+        if (!take.empty()) {
+            out.emplace_back(L, std::move(take));
+            rem.swap(keep);
+            continue;
+        }
+        // no block can take a gate: the cross gates that can go now
+        unsigned nd = 0;
+        L = 0;
+        take.clear();
+        keep.clear();
+        for (auto *g : rem) {
+            unsigned q;
+            if (tile_mask(g, q)) {
+                if (!g->diag) nd |= q;
+                keep.push_back(g);
+            } else if (q & nd) {
+                keep.push_back(g);
+            } else {
+                L |= q;
+                take.push_back(g);
+            }
+        }
+        out.emplace_back(L | kCrossBlock, std::move(take));
         rem.swap(keep);
     }
     return out;
@@ -485,6 +555,21 @@ static int tc_store_cost8(const SetSlots &ss) {
 TcOps tc_ops(const TcBlocks &blocks, bool phases) {
     TcOps out;
     for (const auto &bl : blocks) {
+        if (bl.first & kCrossBlock) {
+            const unsigned lanes = bl.first & ~kCrossBlock;
+            if (!out.empty() && out.back().cross) {
+                out.back().lanes |= lanes;
+                out.back().gates.insert(out.back().gates.end(), bl.second.begin(), bl.second.end());
+                continue;
+            }
+            TcOp op;
+            op.phase = false;
+            op.cross = true;
+            op.lanes = lanes;
+            op.gates = bl.second;
+            out.push_back(std::move(op));
+            continue;
+        }
         bool diag = phases;
         for (auto *g : bl.second) diag = diag && g->diag;
         if (diag && !out.empty() && out.back().phase) {
@@ -502,6 +587,7 @@ TcOps tc_ops(const TcBlocks &blocks, bool phases) {
 }
 
 size_t tc_op_bytes(const TcOp &op) {
+    if (op.cross) return sizeof(TcCrossHdr) + sizeof(TcCrossRec) * op.gates.size();
     return op.phase ? (size_t)8 << __builtin_popcount(op.lanes) : (size_t)2 * 64 * 64 * 2;
 }
 
@@ -555,6 +641,45 @@ static void tc_phase_table(const TcOp &op, const TileLanes &tl, const std::vecto
 static void tc_plan_launch_ordered(const TileLanes &tl, int n, const TcOps &ops, size_t b0,
                                    int nb, TcStageDesc &desc, unsigned char *buf);
 
+// Header and records of a cross op in the layout `lay` it runs in: one record
+// per gate (its two phases as angles), by the tile position of its one lane
+// in the tile (the scalar records last).
+static void tc_cross_records(const TcOp &op, const TileLanes &tl, const TcLayout &lay,
+                             unsigned char *out) {
+    const int m = (int)tl.lanes.size();
+    TcCrossHdr hdr;
+    memset(&hdr, 0, sizeof(hdr));
+    std::vector<std::vector<TcCrossRec>> bucket(m + 1);
+    for (const PendingGate *g : op.gates) {
+        TcCrossRec r;
+        memset(&r, 0, sizeof(r));
+        r.a0 = (float)std::atan2(g->m.v[1], g->m.v[0]);
+        r.a1 = (float)std::atan2(g->m.v[7], g->m.v[6]);
+        int p = m;
+        if (tl.local_of[g->target] >= 0) {
+            p = tl.local_of[g->target];
+        } else {
+            r.tgt = 1LL << g->target;
+        }
+        for (int c : g->controls) {
+            if (tl.local_of[c] >= 0) p = tl.local_of[c];
+            else r.need |= 1LL << c;
+        }
+        bucket[p].push_back(r);
+    }
+    TcCrossRec *rec = (TcCrossRec *)(out + sizeof(TcCrossHdr));
+    int k = 0;
+    for (int p = 0; p <= m; ++p) {
+        hdr.start[p] = k;
+        for (const TcCrossRec &r : bucket[p]) rec[k++] = r;
+    }
+    for (int p = m + 1; p < 15; ++p) hdr.start[p] = k;
+    hdr.nrec = k;
+    for (int b = 0; b < 8; ++b) hdr.rows[b] = (signed char)lay.rows[b];
+    for (int j = 0; j < 5; ++j) hdr.amps[j] = (signed char)lay.amps[j];
+    memcpy(out, &hdr, sizeof(hdr));
+}
+
 void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int nb,
                     TcStageDesc &desc, unsigned char *buf) {
     // The launch's ops in an order that ends with a dense op leaving tile
@@ -564,10 +689,10 @@ void tc_plan_launch(const TileLanes &tl, int n, const TcOps &ops, size_t b0, int
     TcOps slice(ops.begin() + b0, ops.begin() + b0 + nb);
     int last = -1;
     for (int b = nb - 1; b >= 0 && last < 0; --b)
-        if (!slice[b].phase) last = b;
+        if (tc_dense(slice[b])) last = b;
     if (last >= 0 && (slice[last].lanes & kDirectLow)) {
         for (int x = last - 1; x >= 0; --x) {
-            if (slice[x].phase || (slice[x].lanes & kDirectLow)) continue;
+            if (!tc_dense(slice[x]) || (slice[x].lanes & kDirectLow)) continue;
             bool disjoint = true;
             for (int y = x + 1; y < nb && disjoint; ++y) disjoint = !(slice[y].lanes & slice[x].lanes);
             if (disjoint) {
@@ -592,11 +717,14 @@ static void tc_plan_launch_ordered(const TileLanes &tl, int n, const TcOps &ops,
     for (int j = 0; j < desc.nins; ++j) desc.ins_pos[j] = tl.lanes[j];
     desc.nblocks = nb;
     {
-        // operand offsets: dense ops first (16 KB each), then the phase tables
+        // operand offsets: dense ops first (16 KB each, keeping the 1024-byte
+        // alignment of their swizzled operands), then the cross ops' records,
+        // then the phase tables
         unsigned off = 0;
-        for (int pass = 0; pass < 2; ++pass)
+        auto kind = [&](const TcOp &op) { return tc_dense(op) ? 0 : (op.cross ? 1 : 2); };
+        for (int pass = 0; pass < 3; ++pass)
             for (int b = 0; b < nb; ++b)
-                if (ops[b0 + b].phase == (pass == 1)) {
+                if (kind(ops[b0 + b]) == pass) {
                     desc.op_off[b] = off;
                     off += (unsigned)tc_op_bytes(ops[b0 + b]);
                 }
@@ -604,13 +732,13 @@ static void tc_plan_launch_ordered(const TileLanes &tl, int n, const TcOps &ops,
     }
     auto next_dense = [&](int b) -> int {
         for (int x = b + 1; x < nb; ++x)
-            if (!ops[b0 + x].phase) return x;
+            if (tc_dense(ops[b0 + x])) return x;
         return -1;
     };
-    const int first_dense = ops[b0].phase ? next_dense(0) : 0;
+    const int first_dense = !tc_dense(ops[b0]) ? next_dense(0) : 0;
     int last_dense = -1;
     for (int b = 0; b < nb; ++b)
-        if (!ops[b0 + b].phase) last_dense = b;
+        if (tc_dense(ops[b0 + b])) last_dense = b;
     // Load layout: tile positions 0..3 (the contiguous low lanes) plus one
     // more position p on the warp's thread bits, chosen so that the first
     // dense op's operand stores hit the fewest banks twice.
@@ -657,6 +785,11 @@ static void tc_plan_launch_ordered(const TileLanes &tl, int n, const TcOps &ops,
     std::complex<double> U[1024];
     for (int b = 0; b < nb; ++b) {
         const TcOp &op = ops[b0 + b];
+        if (op.cross) {
+            desc.op_kind[b] = 2;
+            tc_cross_records(op, tl, cur, (unsigned char *)(buf + desc.op_off[b]));
+            continue;
+        }
         if (op.phase) {
             // table index bits: the op's lanes on the warp's thread bits
             // first (a warp then reads few distinct banks), then the others

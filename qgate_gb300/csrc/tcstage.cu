@@ -284,6 +284,82 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tile
             const SetSlots &ss = sset[b];
             unsigned slot = (unsigned)ss.lo[r & 31u] ^ (unsigned)ss.hi[r >> 5];
             if (H == 2 && hh) slot ^= ss.q[4];
+            if (PH && d.op_kind[b] == 2) {
+                // Cross op: per tile, every amplitude's phase is a scalar
+                // times one factor per tile lane (picked by the lane's bit),
+                // from the records' angles and the tile's bits outside the
+                // tile lanes.  Scratch: the group's operand buffer, free
+                // between dense ops (U at [0, m], V at [16, 16 + m], the
+                // register table at [32, 64)).
+                if (!t_ready) {
+                    t_ready = mbar_wait(bb, 0u);
+                    if (!t_ready) atomicOr(&g_tc_status, 1u);
+                }
+                const TcCrossHdr &xh = *(const TcCrossHdr *)(Bs + d.op_off[b]);
+                const TcCrossRec *xr = (const TcCrossRec *)(Bs + d.op_off[b] + sizeof(TcCrossHdr));
+                float2 *xf = (float2 *)Ah;
+                const int nrec = min(max(xh.nrec, 0),
+                                     (int)((d.ops_bytes - d.op_off[b] - sizeof(TcCrossHdr)) /
+                                           sizeof(TcCrossRec)));
+                {
+                    // position p's factors, one warp per position: its lanes
+                    // take the position's records in turn, then a fixed
+                    // shuffle tree sums the angles (the same order every run)
+                    const long long g0 = insert_zeros((idx_t)tl, d.ins_pos, d.nins);
+                    const unsigned wl = lt & 31u;
+                    for (int p = (int)(lt >> 5); p <= m; p += (int)(TG / 32u)) {
+                        const int k0 = min(max(xh.start[p], 0), nrec);
+                        const int k1 = min(p < m ? xh.start[p + 1] : nrec, nrec);
+                        float a0 = 0.f, a1 = 0.f;
+                        for (int k = k0 + (int)wl; k < k1; k += 32) {
+                            const TcCrossRec x = xr[k];
+                            if ((g0 & x.need) != x.need) continue;
+                            if (x.tgt == 0) {
+                                a0 += x.a0;
+                                a1 += x.a1;
+                            } else {
+                                a1 += (g0 & x.tgt) ? x.a1 : x.a0;
+                            }
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+                            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+                        }
+                        if (wl == 0u) {
+                            constexpr float kTwoPi = 6.283185307f;
+                            a0 -= kTwoPi * rintf(a0 * (1.f / kTwoPi));
+                            a1 -= kTwoPi * rintf(a1 * (1.f / kTwoPi));
+                            float s0, c0, s1, c1;
+                            sincosf(a0, &s0, &c0);
+                            sincosf(a1, &s1, &c1);
+                            xf[p] = make_float2(c0, s0);
+                            xf[16 + p] = make_float2(c1, s1);
+                        }
+                    }
+                }
+                group_sync(gbar, TG);
+                if (lt < 32u) {
+                    float2 f = make_float2(1.f, 0.f);
+#pragma unroll
+                    for (int k = 0; k < 5; ++k)
+                        f = cmul(f, xf[(lt >> k & 1u) ? 16 + xh.amps[k] : xh.amps[k]]);
+                    xf[32 + lt] = f;
+                }
+                float2 base = xf[16 + m];  // the scalar
+                for (int bb2 = 0; bb2 < t; ++bb2)
+                    base = cmul(base, xf[(r >> bb2 & 1u) ? 16 + xh.rows[bb2] : xh.rows[bb2]]);
+                group_sync(gbar, TG);
+#pragma unroll
+                for (int j = 0; j < NA; ++j) {
+                    const float2 f = cmul(base, xf[32 + ((H == 2 && hh) ? (j | 16) : j)]);
+                    const float x = __uint_as_float(v[2 * j]), y = __uint_as_float(v[2 * j + 1]);
+                    v[2 * j] = __float_as_uint(fmaf(x, f.x, -y * f.y));
+                    v[2 * j + 1] = __float_as_uint(fmaf(x, f.y, y * f.x));
+                }
+                group_sync(gbar, TG);  // the scratch is read before the next split
+                continue;
+            }
             if (PH && d.op_kind[b] == 1) {
                 // Phase op: each amplitude times its table entry, in place
                 // (the layout stays).  Every thread waits for the operands
@@ -472,9 +548,13 @@ void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool 
     for (int b = 0; b < d.nblocks + 2; ++b) {
         const unsigned any = reach(d.sets[b]);
         const bool phase = b < d.nblocks && d.op_kind[b] == 1;
+        const bool cross = b < d.nblocks && d.op_kind[b] == 2;
+        if (b < d.nblocks && d.op_kind[b] > 2) fail(2, "tensor stage: op %d of unknown kind", b);
         if (!phase && any >= (1u << d.m)) fail(2, "tensor stage: slot table %d outside the tile", b);
         if (b >= d.nblocks) continue;
-        const unsigned need = phase ? 8u * (any + 1u) : 2u * 64u * 64u * 2u;
+        // (a cross op's records are bounded by the operand array in the kernel)
+        const unsigned need = phase ? 8u * (any + 1u)
+                                    : (cross ? (unsigned)sizeof(TcCrossHdr) : 2u * 64u * 64u * 2u);
         if ((d.op_off[b] & 15u) != 0 || d.op_off[b] + need > d.ops_bytes)
             fail(2, "tensor stage: op %d operands outside the operand array", b);
     }
@@ -491,8 +571,8 @@ void launch_tstage(void *state, const TcStageDesc &d, cudaStream_t stream, bool 
         const int ctas = std::min((tiles + groups - 1) / groups, sms);
         kern<<<(unsigned)ctas, threads, smem, stream>>>((float2 *)state, d, tiles);
     };
-    bool phases = false;
-    for (int b = 0; b < d.nblocks; ++b) phases = phases || d.op_kind[b] == 1;
+    bool phases = false;  // phase or cross ops
+    for (int b = 0; b < d.nblocks; ++b) phases = phases || d.op_kind[b] != 0;
     if (d.m == 12 && two_per_row)
         phases ? launch(k_tstage<1, 3, 2, true>, 3, 768) : launch(k_tstage<1, 3, 2, false>, 3, 768);
     else if (d.m == 12)

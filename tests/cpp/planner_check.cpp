@@ -36,8 +36,9 @@ static std::vector<PendingGate> random_gates(std::mt19937 &rng, int n, int count
             if (x != t && std::find(c.begin(), c.end(), x) == c.end()) c.push_back(x);
         }
         const double th = U(rng), ph = U(rng), la = U(rng);
-        if ((int)(rng() % 4) >= dense_in_4)  // diagonal
-            out.push_back(make_gate(t, c, 1., 0., 0., std::polar(1., ph)));
+        if ((int)(rng() % 4) >= dense_in_4)  // diagonal: a controlled phase or an Rz
+            out.push_back(make_gate(t, c, rng() % 2 ? std::polar(1., -la) : cd(1., 0.), 0., 0.,
+                                    std::polar(1., ph)));
         else
             out.push_back(make_gate(t, c, std::cos(th / 2), -std::polar(std::sin(th / 2), la),
                                     std::polar(std::sin(th / 2), ph),
@@ -100,9 +101,13 @@ int main(int argc, char **argv) {
     }
     // stage_take / plan_stage_lanes / tc_blocks on random gate lists.
     int bad_partition = 0, bad_commute = 0, bad_count = 0, bad_lanes = 0, bad_blocks = 0;
+    int cross_taken = 0;
     for (int trial = 0; trial < 40; ++trial) {
         const int n = 16 + (int)(rng() % 10), M = 12;
-        auto gates = random_gates(rng, n, 200 + (int)(rng() % 400));
+        // odd trials: cross gates allowed, and mostly diagonal gates
+        const bool cross = trial % 2 == 1;
+        const int cap = cross ? kMaxTensorStageGates : kMaxStageGates;
+        auto gates = random_gates(rng, n, 200 + (int)(rng() % 400), cross ? 2 : 3);
         std::vector<const PendingGate *> rem;
         for (auto &g : gates) rem.push_back(&g);
         const unsigned long long base = 15;
@@ -112,17 +117,23 @@ int main(int argc, char **argv) {
                 rem.erase(rem.begin());
                 continue;
             }
-            const unsigned long long S = plan_stage_lanes(rem, base, M);
+            const unsigned long long S = plan_stage_lanes(rem, base, M, cross, cap);
             if (__builtin_popcountll(S) > M || (S & (base | q0)) != (base | q0)) ++bad_lanes;
             // the fast count equals stage_take's over the window, for S and neighbours
             std::vector<unsigned long long> qw;
-            for (size_t i = 0; i < rem.size() && i < 512; ++i) qw.push_back(gate_qmask(*rem[i]));
+            std::vector<char> xd;
+            for (size_t i = 0; i < rem.size() && i < 512; ++i) {
+                qw.push_back(gate_qmask(*rem[i]));
+                xd.push_back(cross && unit_diag(*rem[i]));
+            }
             for (int v = 0; v < 4; ++v) {
                 const unsigned long long T = v == 0 ? S : (S ^ (1ULL << (rng() % n)));
-                if (take_count(qw, T) != stage_take(rem, T, 512, nullptr, nullptr)) ++bad_count;
+                if (take_count(qw, xd, T, cross, cap) !=
+                    stage_take(rem, T, 512, nullptr, nullptr, cross, cap))
+                    ++bad_count;
             }
             std::vector<const PendingGate *> take, keep;
-            stage_take(rem, S, rem.size(), &take, &keep);
+            stage_take(rem, S, rem.size(), &take, &keep, cross, cap);
             // partition in order, taken gates inside S, nothing taken past a
             // deferred gate that shares a lane with it
             size_t it = 0, ik = 0;
@@ -131,8 +142,9 @@ int main(int argc, char **argv) {
                 const unsigned long long q = gate_qmask(*g);
                 if (it < take.size() && take[it] == g) {
                     ++it;
-                    if (q & ~S) ++bad_lanes;
+                    if ((q & ~S) && !(cross && cross_gate(*g, S))) ++bad_lanes;
                     if (q & blocked) ++bad_commute;
+                    cross_taken += (q & ~S) != 0;
                 } else if (ik < keep.size() && keep[ik] == g) {
                     ++ik;
                     blocked |= q;
@@ -148,27 +160,39 @@ int main(int argc, char **argv) {
                 auto blocks = tc_blocks(take, tl);
                 std::vector<const PendingGate *> seq;
                 for (auto &b : blocks) {
-                    if (__builtin_popcount(b.first) > 5) ++bad_blocks;
+                    const bool xb = (b.first & kCrossBlock) != 0;
+                    const unsigned bl = b.first & ~kCrossBlock;
+                    if (!xb && __builtin_popcount(bl) > 5) ++bad_blocks;
                     for (auto *g : b.second) {
-                        unsigned q = 1u << tl.local_of[g->target];
-                        for (int c : g->controls) q |= 1u << tl.local_of[c];
-                        if (q & ~b.first) ++bad_blocks;
+                        unsigned q = 0;
+                        bool in = true;
+                        for (int x : g->controls)
+                            if (tl.local_of[x] >= 0) q |= 1u << tl.local_of[x]; else in = false;
+                        if (tl.local_of[g->target] >= 0) q |= 1u << tl.local_of[g->target];
+                        else in = false;
+                        // a cross block holds gates with a lane outside the
+                        // tile and at most one inside; other blocks in-tile gates
+                        if (in == xb || (q & ~bl) || (xb && __builtin_popcount(q) > 1)) ++bad_blocks;
                         seq.push_back(g);
                     }
                 }
                 // the block order is a commutation-safe reordering of `take`
+                // (gates on common lanes keep their order unless both are diagonal)
                 for (size_t a = 0; a < seq.size(); ++a)
                     for (size_t b2 = a + 1; b2 < seq.size(); ++b2) {
                         const auto pa = std::find(take.begin(), take.end(), seq[a]) - take.begin();
                         const auto pb = std::find(take.begin(), take.end(), seq[b2]) - take.begin();
-                        if (pa > pb && (gate_qmask(*seq[a]) & gate_qmask(*seq[b2]))) ++bad_blocks;
+                        if (pa > pb && (gate_qmask(*seq[a]) & gate_qmask(*seq[b2])) &&
+                            !(seq[a]->diag && seq[b2]->diag))
+                            ++bad_blocks;
                     }
             }
             rem.swap(keep);
         }
     }
-    printf("bad_partition %d\nbad_commute %d\nbad_count %d\nbad_lanes %d\nbad_blocks %d\n",
-           bad_partition, bad_commute, bad_count, bad_lanes, bad_blocks);
+    printf("bad_partition %d\nbad_commute %d\nbad_count %d\nbad_lanes %d\nbad_blocks %d\n"
+           "cross_taken %d\n",
+           bad_partition, bad_commute, bad_count, bad_lanes, bad_blocks, cross_taken);
     // Operand slots of random layouts are bijections of the 4096 tile indices,
     // and a launch plan's slot tables address every slot once per layout.
     {
@@ -184,7 +208,8 @@ int main(int argc, char **argv) {
             for (unsigned ti = 0; ti < 4096; ++ti) seen.insert(tc_operand_slot(L, ti));
             if (seen.size() != 4096 || *seen.rbegin() >= 4096) ++bad_slots;
         }
-        int bad_tables = 0, launches = 0, phase_ops = 0, dense_ops = 0, direct_launches = 0;
+        int bad_tables = 0, launches = 0, phase_ops = 0, dense_ops = 0, direct_launches = 0,
+            cross_ops = 0;
         double worst_emul = 0.;
         auto b_index = [](int k, int nn) {  // the FP16 index of B[k][n] in Bh (Bl: + 4096)
             return (size_t)(k / 16) * 1024 + (k % 16 / 8) * 512 + (nn / 8) * 64 + (nn % 8) * 8 + k % 8;
@@ -196,12 +221,17 @@ int main(int argc, char **argv) {
             std::vector<const PendingGate *> rem;
             for (auto &g : gates) rem.push_back(&g);
             const unsigned long long base = 15;
-            const unsigned long long S0 = plan_stage_lanes(rem, base, m);
+            // trials 1, 3 mod 4: cross gates allowed (as the gate queue plans)
+            const bool cross = trial % 4 == 1 || trial % 4 == 3;
+            const int cap = cross ? kMaxTensorStageGates : kMaxStageGates;
+            const unsigned long long S0 = plan_stage_lanes(rem, base, m, cross, cap);
             std::vector<const PendingGate *> take, keep;
-            stage_take(rem, S0, rem.size(), &take, &keep);
+            stage_take(rem, S0, rem.size(), &take, &keep, cross, cap);
             if (take.size() < 2) continue;
             unsigned long long SS = S0;
             for (int q = 0; q < n && __builtin_popcountll(SS) < m; ++q) SS |= 1ULL << q;
+            // the tile: random bits on the lanes outside it
+            const long long g0 = (long long)(rng() & ((1u << n) - 1)) & ~(long long)SS;
             TileLanes tl = tile_lanes_of(SS, n);
             const TcOps ops = tc_ops(tc_blocks(take, tl), true);
             const int nb = tc_ops_per_launch(ops, 0);
@@ -217,17 +247,33 @@ int main(int argc, char **argv) {
             };
             // dense ops and the natural tile: TR rows x 32 registers onto the
             // tile's slots once; phase ops: onto the table entries equally often
+            // (the launch may order its ops differently from `ops`: every
+            // check here reads the descriptor)
             for (int b = 0; b < nb + 2; ++b) {
-                const bool phase = b < nb && desc.op_kind[b] == 1;
-                if (b < nb) {
-                    (phase ? phase_ops : dense_ops) += 1;
-                    if (desc.op_off[b] % 16 || desc.op_off[b] + tc_op_bytes(ops[b]) > desc.ops_bytes)
+                const int kind = b < nb ? desc.op_kind[b] : 0;
+                if (b < nb && desc.op_off[b] % 16) ++bad_tables;
+                if (kind == 2) {
+                    // cross op: header and records inside the operand array
+                    ++cross_ops;
+                    TcCrossHdr hdr;
+                    memcpy(&hdr, buf + desc.op_off[b], sizeof(hdr));
+                    if (desc.op_off[b] + sizeof(hdr) + sizeof(TcCrossRec) * (size_t)hdr.nrec >
+                        desc.ops_bytes)
                         ++bad_tables;
+                    for (int p = 0; p < m; ++p)
+                        if (hdr.start[p] > hdr.start[p + 1] || hdr.start[p + 1] > hdr.nrec)
+                            ++bad_tables;
+                    continue;
                 }
+                const bool phase = kind == 1;
+                if (b < nb) (phase ? phase_ops : dense_ops) += 1;
                 std::map<unsigned, int> seen;
                 for (unsigned r = 0; r < (unsigned)TR; ++r)
                     for (unsigned j = 0; j < 32; ++j) seen[slot_of(desc.sets[b], r, j)] += 1;
-                const size_t entries = phase ? tc_op_bytes(ops[b]) / 8 : (size_t)1 << m;
+                const size_t entries = phase ? seen.size() : (size_t)1 << m;
+                if (phase && (entries & (entries - 1))) ++bad_tables;
+                if (b < nb && desc.op_off[b] + (phase ? 8 * entries : (size_t)16384) > desc.ops_bytes)
+                    ++bad_tables;
                 if (seen.size() != entries || seen.rbegin()->first >= entries) ++bad_tables;
                 for (auto &kv : seen)
                     if (kv.second != (int)(((size_t)1 << m) / entries)) ++bad_tables;
@@ -240,7 +286,7 @@ int main(int argc, char **argv) {
             std::map<long long, cd> want;
             std::normal_distribution<double> gauss(0, 1);
             auto load_off = [&](unsigned r, unsigned j) {
-                long long lo = desc.dep_hi[j];
+                long long lo = desc.dep_hi[j] | g0;
                 for (int b = 0; b < t; ++b)
                     if (r >> b & 1u) lo |= 1LL << desc.row_lane[b];
                 return lo;
@@ -252,6 +298,35 @@ int main(int argc, char **argv) {
             if (want.size() != ((size_t)1 << m)) ++bad_tables;
             for (int b = 0; b < nb; ++b) {
                 const SetSlots &ss = desc.sets[b];
+                if (desc.op_kind[b] == 2) {
+                    // cross op: per-position angles from the records and the
+                    // tile's outside bits, then every amplitude's phase
+                    TcCrossHdr hdr;
+                    memcpy(&hdr, buf + desc.op_off[b], sizeof(hdr));
+                    const TcCrossRec *rec = (const TcCrossRec *)(buf + desc.op_off[b] + sizeof(hdr));
+                    std::vector<double> A0(m + 1, 0.), A1(m + 1, 0.);
+                    for (int p = 0; p <= m; ++p)
+                        for (int k = hdr.start[p]; k < (p < m ? hdr.start[p + 1] : hdr.nrec); ++k) {
+                            const TcCrossRec &x = rec[k];
+                            if ((g0 & x.need) != x.need) continue;
+                            if (x.tgt == 0) {
+                                A0[p] += x.a0;
+                                A1[p] += x.a1;
+                            } else {
+                                A1[p] += (g0 & x.tgt) ? x.a1 : x.a0;
+                            }
+                        }
+                    for (unsigned r = 0; r < (unsigned)TR; ++r)
+                        for (unsigned j = 0; j < 32; ++j) {
+                            double ph = A1[m];
+                            for (int bb = 0; bb < t; ++bb)
+                                ph += (r >> bb & 1u) ? A1[hdr.rows[bb]] : A0[hdr.rows[bb]];
+                            for (int k = 0; k < 5; ++k)
+                                ph += (j >> k & 1u) ? A1[hdr.amps[k]] : A0[hdr.amps[k]];
+                            V[r][j] *= std::polar(1., ph);
+                        }
+                    continue;
+                }
                 if (desc.op_kind[b] == 1) {
                     const float *tab = (const float *)(buf + desc.op_off[b]);
                     for (unsigned r = 0; r < (unsigned)TR; ++r)
@@ -293,7 +368,7 @@ int main(int argc, char **argv) {
                 ++direct_launches;
                 std::map<long long, int> hit;
                 for (unsigned r = 0; r < (unsigned)TR; ++r) {
-                    long long ro = 0;
+                    long long ro = g0;
                     for (int b = 0; b < t; ++b)
                         if (r >> b & 1u) ro |= 1LL << desc.out_row_lane[b];
                     // a warp's rows cover whole 128-byte lines (lanes 0..3)
@@ -327,6 +402,11 @@ int main(int argc, char **argv) {
                     for (int c : g->controls) cm |= 1LL << c;
                     const cd m00(g->m.v[0], g->m.v[1]), m01(g->m.v[2], g->m.v[3]),
                         m10(g->m.v[4], g->m.v[5]), m11(g->m.v[6], g->m.v[7]);
+                    if (g->diag) {  // elementwise (its lanes may lie outside the tile)
+                        for (auto &kv : want)
+                            if ((kv.first & cm) == cm) kv.second *= (kv.first & tb) ? m11 : m00;
+                        continue;
+                    }
                     for (auto &kv : want) {
                         const long long off = kv.first;
                         if ((off & tb) || (off & cm) != cm) continue;
@@ -340,8 +420,8 @@ int main(int argc, char **argv) {
             for (auto &kv : want)
                 worst_emul = std::max(worst_emul, std::abs(got[kv.first] - kv.second) / nrm);
         }
-        printf("emulated_stage_max_rel_err %.3e\nphase_ops %d\ndense_ops %d\n", worst_emul,
-               phase_ops, dense_ops);
+        printf("emulated_stage_max_rel_err %.3e\nphase_ops %d\ndense_ops %d\ncross_ops %d\n",
+               worst_emul, phase_ops, dense_ops, cross_ops);
         printf("bad_slots %d\nbad_tables %d\nlaunches_checked %d\ndirect_out_launches %d\n",
                bad_slots, bad_tables, launches, direct_launches);
     }

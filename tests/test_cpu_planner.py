@@ -55,9 +55,15 @@ def test_split_operands_accuracy(planner_run):
 
 
 def test_stage_planner_invariants(planner_run):
+    """Stage lane sets, gate partitions and fused blocks on random gate lists,
+    half of them with cross gates allowed (diagonal gates with at most one
+    lane in the tile, taken as per-tile phases): taken gates fit the tile or
+    are cross gates, nothing moves past a deferred gate it shares a lane with,
+    and blocks reorder gates only where they commute."""
     vals, _ = planner_run
     for k in ('bad_partition', 'bad_commute', 'bad_count', 'bad_lanes', 'bad_blocks'):
         assert int(vals[k]) == 0, k
+    assert int(vals['cross_taken']) > 0
 
 
 def test_operand_slot_tables_are_bijections(planner_run):
@@ -69,8 +75,8 @@ def test_operand_slot_tables_are_bijections(planner_run):
 
 def test_emulated_stage_matches_the_gates(planner_run):
     """The tensor-stage kernel's data flow emulated in FP64 from launch plans
-    (load layout, slot tables, Bh + Bl operands or phase tables, natural tile
-    or the direct row stores)
+    (load layout, slot tables, Bh + Bl operands, phase tables or cross
+    records, natural tile or the direct row stores)
     equals the plans' gates applied to the tile, for 12- and 13-lane tiles
     with dense and phase ops; what remains is the operands' FP16 split (~2^-22
     per op) and the compensation scale (~1e-7 per dense op)."""
@@ -81,3 +87,6 @@ def test_emulated_stage_matches_the_gates(planner_run):
     # leaves lanes 0 and 1 to the rows) and ones through the natural tile
     direct = int(vals['direct_out_launches'])
     assert 0 < direct < int(vals['launches_checked'])
+    # cross ops (per-tile phases from gates with lanes outside the tile),
+    # emulated on a tile with random bits outside it
+    assert int(vals['cross_ops']) > 0
