@@ -198,6 +198,19 @@ def _family(name, rng, n, layers):
                 a, b = (int(x) for x in rng.choice(n, 2, replace=False))
                 ops.append(('g', 'U1', (float(rng.uniform(-np.pi, np.pi)),), False, a, (b,)))
             ops += [('g', 'H', (), False, int(q), ()) for q in rng.choice(n, 3, replace=False)]
+        elif name == 'multi_control_diagonal':
+            # H on a third of the qubits, then diagonal gates with one to three
+            # controls (CZ, CU1, controlled RZ, CCZ-like U1): most of them reach
+            # outside any tile and run as per-tile phases (cross ops)
+            ops += [('g', 'H', (), False, int(q), ()) for q in rng.choice(n, n // 3, replace=False)]
+            for _k in range(n):
+                lanes = [int(x) for x in rng.choice(n, 4, replace=False)]
+                nc = int(rng.integers(1, 4))
+                kind = int(rng.integers(0, 3))
+                g = (('Z', ()) if kind == 0 else
+                     ('U1', (float(rng.uniform(-np.pi, np.pi)),)) if kind == 1 else
+                     ('RZ', (float(rng.uniform(-np.pi, np.pi)),)))
+                ops.append(('g', g[0], g[1], False, lanes[0], tuple(lanes[1:1 + nc])))
         elif name == 'sparse':
             # CX and Toffoli permutations with a U3 on two qubits: sparse blocks
             for _k in range(n // 2):
@@ -214,19 +227,21 @@ def _family(name, rng, n, layers):
     return ops
 
 
-@pytest.mark.parametrize('family', ['dense_blocks', 'diagonal', 'sparse', 'skewed'])
+@pytest.mark.parametrize('family', ['dense_blocks', 'diagonal', 'sparse', 'skewed',
+                                    'multi_control_diagonal'])
 def test_tensor_stage_accuracy_by_block_family(rt, tensor_mode, family):
     """24 qubits, 24 layers of block families other than the benchmark's
     (dense Haar-like 5-qubit blocks, diagonal-heavy stages that become phase
-    ops, sparse permutation blocks, and a state whose amplitudes span ~17
-    orders of magnitude), complex64 on the tensor-core stages against the
+    and cross ops, multi-controlled diagonal gates reaching outside the tiles,
+    sparse permutation blocks, and a state whose amplitudes span ~17 orders of
+    magnitude), complex64 on the tensor-core stages against the
     oracle's C port in complex128 (cs_run_circuit).  Bars: fidelity error
     |1 - |<psi64|psi32>|| <= 1e-5 and max |p32 - p64| <= 1e-7, the bars of the
     headline circuit."""
     from oracle import cpu_port
     nat = tensor_mode
     rng = np.random.default_rng({'dense_blocks': 51, 'diagonal': 52, 'sparse': 53,
-                                 'skewed': 54}[family])
+                                 'skewed': 54, 'multi_control_diagonal': 55}[family])
     n = 24
     ops = _family(family, rng, n, 24)
     st = cpu_port.State(n, np.complex128)
