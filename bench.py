@@ -657,14 +657,20 @@ def run_c4(args, rt, nat):
         out[label] = res
         return qs
 
-    n1 = args.c4_random_qubits
-    ops1 = circuit(n1, 30, seed_angles=40, seed_perm=40)
+    # the 30-qubit circuit's tuned fusion shape (12-lane tensor stages when
+    # there is none)
     cached = autotune._load().get(autotune._key(30, np.float32))
     if cached:
         autotune.apply(cached)
-    qs = run(n1, ops1, 'random_%dq_depth30' % n1)
-    qs.delete()
-    nat.call('qg_devices_clear')  # return the cached 64 GiB before the 128 GiB state
+    else:
+        nat.set_fusion(12)
+        nat.set_tensor_blocks(True)
+    n1 = args.c4_random_qubits
+    if n1 > 0:  # 0 skips it
+        ops1 = circuit(n1, 30, seed_angles=40, seed_perm=40)
+        qs = run(n1, ops1, 'random_%dq_depth30' % n1)
+        qs.delete()
+        nat.call('qg_devices_clear')  # return the cached 64 GiB before the 128 GiB state
 
     n2 = args.c4_qft_qubits
     qs = run(n2, qft_ops(n2, 41), 'qft_%dq' % n2)
@@ -879,7 +885,7 @@ def main():
     ap.add_argument('--no-batch', action='store_true')
     ap.add_argument('--no-compiled', action='store_true')
     ap.add_argument('--no-c4', action='store_true', help='skip the 33/34-qubit large states')
-    ap.add_argument('--c4-random-qubits', type=int, default=33)
+    ap.add_argument('--c4-random-qubits', type=int, default=33, help='0 skips it')
     ap.add_argument('--c4-qft-qubits', type=int, default=34)
     ap.add_argument('--c4-samples', type=int, default=100_000_000)
     ap.add_argument('--batch-circuits', type=int, default=4096)
