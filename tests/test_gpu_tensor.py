@@ -252,3 +252,33 @@ def test_tensor_stage_accuracy_by_block_family(rt, tensor_mode, family):
     print('%s: fidelity error %.3e, max probability error %.3e' % (family, ferr, perr))
     assert ferr <= 1e-5 and perr <= 1e-7, (family, ferr, perr)
     assert nat.timing_read('tstage')[0] > 0 and nat.tensor_stage_status() == 0
+
+
+@pytest.mark.parametrize('variant', ['tile12', 'tile12_two_per_row', 'tile13'])
+def test_tensor_stage_cross_ops_on_every_variant(rt, tensor_mode, variant):
+    """A 20-qubit QFT plus controlled phases whose lanes span the whole
+    state: the diagonal gates reaching outside the tiles run as per-tile
+    phases (cross ops), so the QFT needs a few passes, not one per ladder;
+    on the default 12-lane variant, the two-threads-per-row variant and the
+    13-lane variant, against the oracle."""
+    nat = tensor_mode
+    tile = 13 if variant == 'tile13' else 12
+    nat.set_fusion_params(nat.PREC_FP32, tile, 5, 0)
+    nat.call('qg_set_stage_pipelining', 1 if variant == 'tile12_two_per_row' else 0)
+    try:
+        rng = np.random.default_rng(61)
+        n = 20
+        ops = [('g', 'X', (), False, q, ()) for q in range(n) if rng.random() < 0.5]
+        for i in range(n):
+            ops.append(('g', 'H', (), False, i, ()))
+            ops += [('g', 'U1', (np.pi / (1 << (j - i)),), False, i, (j,)) for j in range(i + 1, n)]
+        ops += [('g', 'RZ', (float(rng.uniform(-np.pi, np.pi)),), False, int(q), (int(c),))
+                for q, c in rng.integers(0, n, (12, 2)) if q != c]
+        nat.gate_stats(reset=True)
+        got = _run(rt, n, ops)
+        passes = nat.gate_stats(reset=True)['passes']
+    finally:
+        nat.call('qg_set_stage_pipelining', 0)
+    _check(got, sv.run_ops(n, ops, np.complex128))
+    assert passes <= 4, passes
+    assert nat.timing_read('tstage')[0] > 0 and nat.tensor_stage_status() == 0
