@@ -289,8 +289,8 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tile
                 // times one factor per tile lane (picked by the lane's bit),
                 // from the records' angles and the tile's bits outside the
                 // tile lanes.  Scratch: the group's operand buffer, free
-                // between dense ops (U at [0, m], V at [16, 16 + m], the
-                // register table at [32, 64)).
+                // between dense ops (U at [0, m], V at [16, 16 + m]); the
+                // register table lives in the warps' lanes.
                 if (!t_ready) {
                     t_ready = mbar_wait(bb, 0u);
                     if (!t_ready) atomicOr(&g_tc_status, 1u);
@@ -302,16 +302,18 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tile
                                      (int)((d.ops_bytes - d.op_off[b] - sizeof(TcCrossHdr)) /
                                            sizeof(TcCrossRec)));
                 {
-                    // position p's factors, one warp per position: its lanes
-                    // take the position's records in turn, then a fixed
-                    // shuffle tree sums the angles (the same order every run)
+                    // position p's factors, one half-warp per position: its
+                    // lanes take the position's records in turn, then a fixed
+                    // shuffle tree sums the angles (the same order every run);
+                    // both halves of a warp run every round (uniform shuffles)
                     const long long g0 = insert_zeros((idx_t)tl, d.ins_pos, d.nins);
-                    const unsigned wl = lt & 31u;
-                    for (int p = (int)(lt >> 5); p <= m; p += (int)(TG / 32u)) {
-                        const int k0 = min(max(xh.start[p], 0), nrec);
-                        const int k1 = min(p < m ? xh.start[p + 1] : nrec, nrec);
+                    const unsigned wl = lt & 31u, half = wl >> 4, hl = wl & 15u;
+                    for (int p0 = (int)(lt >> 5) * 2; p0 <= m; p0 += (int)(TG / 16u)) {
+                        const int p = p0 + (int)half;
+                        const int k0 = p <= m ? min(max(xh.start[p], 0), nrec) : 0;
+                        const int k1 = p < m ? min(xh.start[p + 1], nrec) : (p == m ? nrec : 0);
                         float a0 = 0.f, a1 = 0.f;
-                        for (int k = k0 + (int)wl; k < k1; k += 32) {
+                        for (int k = k0 + (int)hl; k < k1; k += 16) {
                             const TcCrossRec x = xr[k];
                             if ((g0 & x.need) != x.need) continue;
                             if (x.tgt == 0) {
@@ -322,11 +324,11 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tile
                             }
                         }
 #pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) {
+                        for (int o = 8; o > 0; o >>= 1) {
                             a0 += __shfl_xor_sync(0xffffffffu, a0, o);
                             a1 += __shfl_xor_sync(0xffffffffu, a1, o);
                         }
-                        if (wl == 0u) {
+                        if (hl == 0u && p <= m) {
                             constexpr float kTwoPi = 6.283185307f;
                             a0 -= kTwoPi * rintf(a0 * (1.f / kTwoPi));
                             a1 -= kTwoPi * rintf(a1 * (1.f / kTwoPi));
@@ -339,20 +341,21 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tile
                     }
                 }
                 group_sync(gbar, TG);
-                if (lt < 32u) {
-                    float2 f = make_float2(1.f, 0.f);
+                // (labels as in the kernel's load layout) this thread's row
+                // factor, and lane l of every warp holds register entry l
+                float2 tab = make_float2(1.f, 0.f);
 #pragma unroll
-                    for (int k = 0; k < 5; ++k)
-                        f = cmul(f, xf[(lt >> k & 1u) ? 16 + xh.amps[k] : xh.amps[k]]);
-                    xf[32 + lt] = f;
-                }
+                for (int k = 0; k < 5; ++k)
+                    tab = cmul(tab, xf[((lt & 31u) >> k & 1u) ? 16 + xh.amps[k] : xh.amps[k]]);
                 float2 base = xf[16 + m];  // the scalar
                 for (int bb2 = 0; bb2 < t; ++bb2)
                     base = cmul(base, xf[(r >> bb2 & 1u) ? 16 + xh.rows[bb2] : xh.rows[bb2]]);
-                group_sync(gbar, TG);
 #pragma unroll
                 for (int j = 0; j < NA; ++j) {
-                    const float2 f = cmul(base, xf[32 + ((H == 2 && hh) ? (j | 16) : j)]);
+                    const int src = (H == 2 && hh) ? (j | 16) : j;
+                    const float2 e = make_float2(__shfl_sync(0xffffffffu, tab.x, src),
+                                                 __shfl_sync(0xffffffffu, tab.y, src));
+                    const float2 f = cmul(base, e);
                     const float x = __uint_as_float(v[2 * j]), y = __uint_as_float(v[2 * j + 1]);
                     v[2 * j] = __float_as_uint(fmaf(x, f.x, -y * f.y));
                     v[2 * j + 1] = __float_as_uint(fmaf(x, f.y, y * f.x));
