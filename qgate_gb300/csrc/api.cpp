@@ -455,31 +455,34 @@ static BufPtr kron_factors(Device &d, int prec, std::vector<Factor> fs) {
 // pending).
 static void materialize(Device &d, States *s) {
     if (s->lazy == States::kProduct) {
-        BufPtr b = kron_factors(d, s->prec, s->factors);
+        BufPtr b = kron_factors(d, s->prec, s->factors);  // (s unchanged if this throws)
         s->factors.clear();
         s->lazy = States::kDense;
         set_buffer(s, b);
     } else if (s->lazy == States::kView) {
-        BufPtr par = s->parent;
-        s->parent.reset();
-        s->lazy = States::kDense;
-        if (par.use_count() == 1) {
+        // (s changes only once the new amplitudes are formed: an allocation
+        // that fails leaves the view as it was)
+        if (s->parent.use_count() == 1) {
             // the source is gone: remove the lane in place and keep its buffer
             d.g_inplace += 1;
             timed(d, "measure", [&] {
-                launch_shrink_inplace(s->prec, par->d, s->n_lanes + 1, s->sep_lane, s->sep_value,
-                                      s->sep_norm, d.stream);
+                launch_shrink_inplace(s->prec, s->parent->d, s->n_lanes + 1, s->sep_lane,
+                                      s->sep_value, s->sep_norm, d.stream);
             });
+            BufPtr par = std::move(s->parent);
+            s->lazy = States::kDense;
             set_buffer(s, par);
         } else {
-            d.g_copies += 1;
             BufPtr b = new_buffer(d, s->prec, s->n_lanes);
+            d.g_copies += 1;
             PairIdx pi = pair_pattern({s->sep_lane}, (unsigned long long)s->sep_value << s->sep_lane,
                                       0);
             timed(d, "measure", [&] {
-                launch_shrink(s->prec, b->d, par->d, (idx_t)1 << s->n_lanes, pi, s->sep_norm,
-                              d.stream);
+                launch_shrink(s->prec, b->d, s->parent->d, (idx_t)1 << s->n_lanes, pi,
+                              s->sep_norm, d.stream);
             });
+            s->parent.reset();
+            s->lazy = States::kDense;
             set_buffer(s, b);
         }
     }
