@@ -2291,21 +2291,35 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
     for (auto &P : plans)
         if (!P.error.empty()) fail(QG_ERR_VALUE, "%s", P.error.c_str());
 
-    std::vector<RegOp<float>> ops_all;
-    std::vector<SetSlots> sets_all;
+    // The circuits' programs in one buffer (offsets first, then the copies
+    // in parallel).
+    std::vector<long long> ops_at(n_circuits + 1, 0), sets_at(n_circuits + 1, 0);
+    for (int c = 0; c < n_circuits; ++c) {
+        ops_at[c + 1] = ops_at[c] + (long long)plans[c].ops.size();
+        sets_at[c + 1] = sets_at[c] + (long long)plans[c].sets.size();
+    }
+    if (sets_at[n_circuits] > INT32_MAX) fail(QG_ERR_VALUE, "too many register sets in one batch.");
+    std::vector<RegOp<float>> ops_all((size_t)ops_at[n_circuits]);
+    std::vector<SetSlots> sets_all((size_t)sets_at[n_circuits]);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int c = 0; c < n_circuits; ++c) {
+        std::copy(plans[c].ops.begin(), plans[c].ops.end(), ops_all.begin() + ops_at[c]);
+        std::copy(plans[c].sets.begin(), plans[c].sets.end(), sets_all.begin() + sets_at[c]);
+    }
     std::vector<ResidentCircuit> res[14];
     std::vector<BatchStage> stages;
     std::vector<unsigned> stage_live;
+    // per round, the (stage, tile) items of the per-round form (the
+    // one-launch form needs only the count of rounds)
     std::vector<std::vector<int2>> rounds;
+    const bool per_round = !d.batch_one_launch;
     std::vector<long long> big_off;
     std::vector<int> big_n, big_idx;
     long long arena_elems = 0;
     for (int c = 0; c < n_circuits; ++c) {
         Plan &P = plans[c];
-        const long long ops_base = (long long)ops_all.size();
-        const int sets_base = (int)sets_all.size();
-        ops_all.insert(ops_all.end(), P.ops.begin(), P.ops.end());
-        sets_all.insert(sets_all.end(), P.sets.begin(), P.sets.end());
+        const long long ops_base = ops_at[c];
+        const int sets_base = (int)sets_at[c];
         if (P.resident) {
             ResidentCircuit rc;
             rc.ops_off = ops_base;
@@ -2331,6 +2345,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                 stages.push_back(st);
                 stage_live.push_back(P.stages[r].live);
                 if (rounds.size() <= r) rounds.resize(r + 1);
+                if (!per_round) continue;
                 // the per-round form starts from a zeroed arena: only the
                 // tiles that can hold a nonzero amplitude run
                 const unsigned live = P.stages[r].live;
