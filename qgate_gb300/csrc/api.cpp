@@ -242,6 +242,10 @@ struct Device {
     // Ring of split block operands: pinned host staging and its device copy.
     static constexpr size_t kBRingBytes = 32ull << 20;
     unsigned char *h_bring = nullptr, *d_bring = nullptr;
+    // Pinned staging of a batch's programs (grown on demand; reused by the
+    // next batch, which starts after this one's results are read).
+    unsigned char *h_batch = nullptr;
+    size_t h_batch_bytes = 0;
     size_t bring_off = 0;
     long long n_gates = 0, n_passes = 0, n_bytes = 0;
     // qubit-grouping counters: join calls, kron passes, state buffers
@@ -1447,6 +1451,9 @@ int qg_devices_clear(void) {
         cudaStreamSynchronize(g_dev.stream);
         drop_traces(g_dev);
         g_dev.arena.trim();
+        if (g_dev.h_batch) cudaFreeHost(g_dev.h_batch);
+        g_dev.h_batch = nullptr;
+        g_dev.h_batch_bytes = 0;
     }
     QG_END
 }
@@ -2299,12 +2306,23 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
         sets_at[c + 1] = sets_at[c] + (long long)plans[c].sets.size();
     }
     if (sets_at[n_circuits] > INT32_MAX) fail(QG_ERR_VALUE, "too many register sets in one batch.");
-    std::vector<RegOp<float>> ops_all((size_t)ops_at[n_circuits]);
-    std::vector<SetSlots> sets_all((size_t)sets_at[n_circuits]);
+    // straight into pinned memory, so that their upload is one DMA each
+    const size_t ops_bytes = (size_t)ops_at[n_circuits] * sizeof(RegOp<float>);
+    const size_t sets_bytes = (size_t)sets_at[n_circuits] * sizeof(SetSlots);
+    const size_t stage_bytes = ((ops_bytes + 255) & ~(size_t)255) + sets_bytes;
+    if (d.h_batch_bytes < stage_bytes) {
+        if (d.h_batch) QG_CUDA(cudaFreeHost(d.h_batch));
+        d.h_batch = nullptr;
+        d.h_batch_bytes = 0;
+        QG_CUDA(cudaMallocHost(&d.h_batch, stage_bytes));
+        d.h_batch_bytes = stage_bytes;
+    }
+    RegOp<float> *ops_all = (RegOp<float> *)d.h_batch;
+    SetSlots *sets_all = (SetSlots *)(d.h_batch + ((ops_bytes + 255) & ~(size_t)255));
 #pragma omp parallel for schedule(dynamic, 64)
     for (int c = 0; c < n_circuits; ++c) {
-        std::copy(plans[c].ops.begin(), plans[c].ops.end(), ops_all.begin() + ops_at[c]);
-        std::copy(plans[c].sets.begin(), plans[c].sets.end(), sets_all.begin() + sets_at[c]);
+        std::copy(plans[c].ops.begin(), plans[c].ops.end(), ops_all + ops_at[c]);
+        std::copy(plans[c].sets.begin(), plans[c].sets.end(), sets_all + sets_at[c]);
     }
     std::vector<ResidentCircuit> res[14];
     std::vector<BatchStage> stages;
@@ -2364,8 +2382,8 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     try {
-        auto *d_ops = (RegOp<float> *)up(ops_all.data(), ops_all.size() * sizeof(RegOp<float>));
-        auto *d_sets = (SetSlots *)up(sets_all.data(), sets_all.size() * sizeof(SetSlots));
+        auto *d_ops = (RegOp<float> *)up(ops_all, ops_bytes);
+        auto *d_sets = (SetSlots *)up(sets_all, sets_bytes);
         ResidentCircuit *d_res[14];
         for (int n = 8; n <= 13; ++n)
             d_res[n] = (ResidentCircuit *)up(res[n].data(), res[n].size() * sizeof(ResidentCircuit));
