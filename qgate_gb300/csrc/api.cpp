@@ -25,6 +25,7 @@
 #include <set>
 #include <unordered_map>
 #include <unordered_set>
+#include <unistd.h>
 
 namespace qg {
 
@@ -1060,6 +1061,16 @@ static void host_copy(void *dst, const void *src, size_t bytes) {
 // when the device writes pageable host memory (kernel_output and
 // host_direct), else through the pinned staging buffers in chunks (two in
 // flight), each copied into the host buffer by host threads.
+// The host's page size (one write per page faults a destination in; 64 KB
+// pages on some Arm hosts make 4 KB steps 16 times too many).
+static size_t host_page_bytes() {
+    static const size_t bytes = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v >= 4096 ? (size_t)v : (size_t)4096;
+    }();
+    return bytes;
+}
+
 template <class F>
 static void staged_d2h(Device &d, void *host, idx_t count, size_t item, F produce,
                        bool kernel_output = true) {
@@ -1077,7 +1088,7 @@ static void staged_d2h(Device &d, void *host, idx_t count, size_t item, F produc
             // Touch every page of the destination in parallel while the
             // kernels run (the copy overwrites all of it).
             char *h = (char *)host;
-            const size_t kPage = 4096;
+            const size_t kPage = host_page_bytes();
 #pragma omp parallel for schedule(static)
             for (long long i = 0; i < (long long)((bytes + kPage - 1) / kPage); ++i)
                 ((volatile char *)h)[(size_t)i * kPage] = 0;
@@ -2829,7 +2840,7 @@ int qg_sampling_pool_sample(qg_handle hp, int64_t *obs, int64_t n_samples,
                               (int)p->empty_pos.size(), d.stream);
             });
             char *h = (char *)obs;
-            const size_t kPage = 4096;
+            const size_t kPage = host_page_bytes();
 #pragma omp parallel for schedule(static)
             for (long long i = 0; i < (long long)((bytes + kPage - 1) / kPage); ++i)
                 ((volatile char *)h)[(size_t)i * kPage] = 0;
