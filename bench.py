@@ -876,7 +876,7 @@ def main():
     ap.add_argument('--no-tensor', action='store_true',
                     help='complex64 stages on the CUDA cores (k_rstage) instead of tcgen05 blocks')
     ap.add_argument('--samples', type=int, default=10_000_000)
-    ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--e2e-steps', type=int, default=4)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-fidelity', action='store_true',
                     help='skip the complex64-vs-complex128 accuracy check of the final state')
