@@ -302,42 +302,42 @@ k_tstage(float2 *__restrict__ s, const __grid_constant__ TcStageDesc d, int tile
                                      (int)((d.ops_bytes - d.op_off[b] - sizeof(TcCrossHdr)) /
                                            sizeof(TcCrossRec)));
                 {
-                    // position p's factors, one half-warp per position: its
-                    // lanes take the position's records in turn, then a fixed
-                    // shuffle tree sums the angles (the same order every run);
-                    // both halves of a warp run every round (uniform shuffles)
+                    // position p's factors, one 8-lane group per position
+                    // (TG / 8 >= 16 groups cover the m + 1 <= 14 positions in
+                    // one round): its lanes take the position's records in
+                    // turn, then a fixed shuffle tree sums the angles (the
+                    // same order every run; every lane runs it, so the
+                    // shuffles are uniform), and the group's lanes 0 and 1
+                    // form the two factors
+                    static_assert(TG / 8u >= (unsigned)m + 1u, "one round of positions");
                     const long long g0 = insert_zeros((idx_t)tl, d.ins_pos, d.nins);
-                    const unsigned wl = lt & 31u, half = wl >> 4, hl = wl & 15u;
-                    for (int p0 = (int)(lt >> 5) * 2; p0 <= m; p0 += (int)(TG / 16u)) {
-                        const int p = p0 + (int)half;
-                        const int k0 = p <= m ? min(max(xh.start[p], 0), nrec) : 0;
-                        const int k1 = p < m ? min(xh.start[p + 1], nrec) : (p == m ? nrec : 0);
-                        float a0 = 0.f, a1 = 0.f;
-                        for (int k = k0 + (int)hl; k < k1; k += 16) {
-                            const TcCrossRec x = xr[k];
-                            if ((g0 & x.need) != x.need) continue;
-                            if (x.tgt == 0) {
-                                a0 += x.a0;
-                                a1 += x.a1;
-                            } else {
-                                a1 += (g0 & x.tgt) ? x.a1 : x.a0;
-                            }
+                    const int p = (int)(lt >> 3);
+                    const unsigned ql = lt & 7u;
+                    const int k0 = p <= m ? min(max(xh.start[p], 0), nrec) : 0;
+                    const int k1 = p < m ? min(xh.start[p + 1], nrec) : (p == m ? nrec : 0);
+                    float a0 = 0.f, a1 = 0.f;
+                    for (int k = k0 + (int)ql; k < k1; k += 8) {
+                        const TcCrossRec x = xr[k];
+                        if ((g0 & x.need) != x.need) continue;
+                        if (x.tgt == 0) {
+                            a0 += x.a0;
+                            a1 += x.a1;
+                        } else {
+                            a1 += (g0 & x.tgt) ? x.a1 : x.a0;
                         }
+                    }
 #pragma unroll
-                        for (int o = 8; o > 0; o >>= 1) {
-                            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-                            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-                        }
-                        if (hl == 0u && p <= m) {
-                            constexpr float kTwoPi = 6.283185307f;
-                            a0 -= kTwoPi * rintf(a0 * (1.f / kTwoPi));
-                            a1 -= kTwoPi * rintf(a1 * (1.f / kTwoPi));
-                            float s0, c0, s1, c1;
-                            sincosf(a0, &s0, &c0);
-                            sincosf(a1, &s1, &c1);
-                            xf[p] = make_float2(c0, s0);
-                            xf[16 + p] = make_float2(c1, s1);
-                        }
+                    for (int o = 4; o > 0; o >>= 1) {
+                        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+                        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+                    }
+                    if (ql < 2u && p <= m) {
+                        constexpr float kTwoPi = 6.283185307f;
+                        float a = ql ? a1 : a0;
+                        a -= kTwoPi * rintf(a * (1.f / kTwoPi));
+                        float sa, ca;
+                        sincosf(a, &sa, &ca);
+                        xf[16 * ql + p] = make_float2(ca, sa);
                     }
                 }
                 group_sync(gbar, TG);
