@@ -924,11 +924,48 @@ static bool lookahead_params(const Device &d, const States *s, int &M, unsigned 
 // the caller is still enqueueing the rest of the circuit.
 constexpr size_t kStreamAt = 640;
 
+// X gates (any controls) that reach a basis state before every other gate
+// on their lanes permute it: while a states object is a product of basis
+// factors, such gates are applied to the basis value (exactly; no pass), and
+// the other gates keep their order.  A gate is taken only when no gate kept
+// before it touches its lanes, so it commutes with all of those.  (A circuit
+// that prepares its input with X gates - the QFT of |x> - then plans as if
+// it started from |x>: the prepared lanes no longer hold back the per-tile
+// phases of their controlled phase gates.)
+static void absorb_basis_flips(States *s) {
+    if (s->lazy != States::kProduct || s->pending.empty() || s->n_lanes > 62) return;
+    for (const Factor &f : s->factors)
+        if (f.buf) return;
+    unsigned long long b = 0;  // factors[0] at the highest lanes
+    for (const Factor &f : s->factors) b = (b << f.n_lanes) | (unsigned long long)f.basis;
+    unsigned long long touched = 0;
+    std::vector<PendingGate> keep;
+    keep.reserve(s->pending.size());
+    bool any = false;
+    for (PendingGate &g : s->pending) {
+        unsigned long long lanes = 1ULL << g.target;
+        for (int c : g.controls) lanes |= 1ULL << c;
+        if (!(lanes & touched) && is_x(g.m)) {
+            bool on = true;
+            for (int c : g.controls) on = on && ((b >> c) & 1ULL);
+            if (on) b ^= 1ULL << g.target;
+            any = true;
+            continue;
+        }
+        touched |= lanes;
+        keep.push_back(std::move(g));
+    }
+    s->pending.swap(keep);  // (the kept gates were moved out of the list)
+    if (any) set_basis(s, (long long)b);
+}
+
 static void stream_flush(States *s) {
     Device &d = dev();
     int M;
     unsigned long long base;
     if (s->pending.size() < kStreamAt || !lookahead_params(d, s, M, base)) return;
+    absorb_basis_flips(s);
+    if (s->pending.size() < kStreamAt) return;
     prepare_write(d, s);
     merge_runs(s->pending);
     std::vector<const PendingGate *> remaining;
@@ -951,6 +988,7 @@ static void stream_flush(States *s) {
 static bool replay_trace(Device &d, States *s);
 
 static void flush(States *s) {
+    absorb_basis_flips(s);
     if (s->pending.empty()) {
         s->streamed = false;
         if (s->lazy != States::kDense) materialize(dev(), s);
@@ -1566,14 +1604,11 @@ int qg_qubit_processor_reset_qubit_states(qg_handle hp, qg_handle hs) {
     lookup(g_dev.procs, hp, "processor");
     States *s = get_alloc_states(hs);
     s->pending.clear();
-    if (s->buf && s->buf.use_count() == 1) {
-        // keep the buffer (the common reset of a live state): |0...0> now
-        Device &d = dev();
-        s->lazy = States::kDense;
-        timed(d, "init", [&] { launch_init_basis(s->prec, s->d, (idx_t)1 << s->n_lanes, d.stream); });
-    } else {
-        set_basis(s, 0);
-    }
+    // |0...0> is left lazy, so that gates reaching the basis state first can
+    // still be folded into it; a live state's buffer goes back to the arena
+    // and its free list normally hands the same block back when the state is
+    // next formed.
+    set_basis(s, 0);
     QG_END
 }
 

@@ -260,3 +260,40 @@ def test_lazy_products_read_by_getter_pool_and_compiled_runs(rt, dtype):
     assert np.allclose(c.get_raw(), want_c, atol=4 * ATOL[dtype])
     for x in parts + [a, b, c]:
         x.delete()
+
+
+@pytest.mark.parametrize('dtype', DTYPES, ids=IDS)
+def test_x_gates_on_a_basis_state_fold_into_it(rt, dtype):
+    """X gates (with or without controls) that reach a reset state before any
+    other gate on their lanes are applied to its basis value: a circuit of
+    such gates alone takes no pass and gives the exact basis state; mixed
+    with other gates (an X after an H on its lane, an X whose control saw an
+    earlier gate, controls at 0 and at 1, an adjoint X) and after a reset of
+    a live state, the result still matches the oracle."""
+    from qgate_gb300 import _native as nat
+    n = 9
+    flips = [('g', 'X', (), False, 3, ()), ('g', 'X', (), False, 5, (3,)),
+             ('g', 'X', (), True, 1, (3, 5)), ('g', 'X', (), False, 7, (6,)),
+             ('g', 'X', (), False, 8, (6, 3))]
+    want = sv.run_ops(n, flips)
+    assert abs(want[(1 << 1) | (1 << 3) | (1 << 5)]) == 1.
+    qs = new_state(rt, n, dtype)
+    nat.gate_stats(reset=True)
+    apply_ops(qs, flips)
+    got = qs.get_raw()
+    assert nat.gate_stats(reset=True)['passes'] == 0
+    assert np.array_equal(got, want.astype(got.dtype))
+    rng = np.random.default_rng(46)
+    mixed = ([('g', 'H', (), False, 0, ()), ('g', 'X', (), False, 0, ()),
+              ('g', 'X', (), False, 2, (0,)), ('g', 'X', (), False, 4, ())] + flips +
+             random_ops(rng, n, 30) + [('g', 'X', (), False, 6, ())])
+    qs2 = new_state(rt, n, dtype)
+    apply_ops(qs2, mixed)
+    assert np.allclose(qs2.get_raw(), sv.run_ops(n, mixed), atol=4 * ATOL[dtype])
+    qs2.processor.reset_qubit_states(qs2)
+    nat.gate_stats(reset=True)
+    apply_ops(qs2, flips + mixed)
+    assert np.allclose(qs2.get_raw(), sv.run_ops(n, flips + mixed), atol=4 * ATOL[dtype])
+    assert nat.gate_stats(reset=True)['passes'] > 0
+    for x in (qs, qs2):
+        x.delete()
