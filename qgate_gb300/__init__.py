@@ -11,7 +11,7 @@ runtime plugin protocol.
 * Beyond the runtime protocol: `compiled` (a gate table applied in one call,
   CUDA-graph replay), `qasm` (OpenQASM 2.0 programs lowered to compiled
   circuits), `adjoint` (batched adjoint gradients), `batch` (many small
-  circuits in one launch sequence), `autotune` (fused-stage shapes).
+  circuits in one persistent launch), `autotune` (fused-stage shapes).
 """
 
 __all__ = ['simulator']
