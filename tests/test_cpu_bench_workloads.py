@@ -46,3 +46,20 @@ def test_qft_case_gives_uniform_probabilities():
     assert sum(1 for o in ops if o[0] == 'U1') == n * (n - 1) // 2
     psi = sv.run_ops(n, [('g', nm, a, False, t, c) for nm, a, t, c in ops])
     assert np.allclose(np.abs(psi) ** 2, 1. / (1 << n), atol=1e-12)
+
+
+def test_reference_arm_line_carries_the_shared_config(capsys):
+    """The reference arm's line (the oracle's C port on host cores) reports
+    the same `config` object as the GPU arm's: the workload and the metric's
+    definition, no measured figures."""
+    import argparse
+    import json
+    args = argparse.Namespace(qubits=12, depth=20, dtype='c64', steps=1, warmup=0, gpus=1,
+                              ref_gates=45)
+    bench.run_reference(args)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line['impl'] == 'reference'
+    assert line['config'] == bench.config_block(args)
+    assert line['metric'] == bench.METRIC and line['value'] > 0
+    assert line['e2e']['h2d_bytes_per_step'] == 0 and line['e2e']['d2h_bytes_per_step'] == 0
+    assert line['cpu_baseline']['kind'] == 'port' and line['cpu_baseline']['cores'] >= 1
