@@ -35,6 +35,15 @@ Conventions (OpenQASM 2.0): U(t, p, l) = [[cos(t/2), -e^{il} sin(t/2)],
 rz(p) = u1(p); crz(l) is the controlled diag(e^{-il/2}, e^{il/2}); cu3 and
 cu1 are the controlled u3 and u1 with no extra phase.  Lane i of the engine
 state is qubit i in declaration order of the qregs.
+
+The reference's translation maps `U`, `u3` and `u2` to qgate's U3 and U2
+(qgate/openqasm/formatter.py:71-76), whose matrices carry an extra global
+phase e^{-i(phi+lambda)/2} (qgate/simulator/src/GateMatrix.cpp:13-15): the
+same program gives the same probabilities, samples and measurement outcomes
+here, and amplitudes that differ from the reference's by that global phase.
+Expressions follow OpenQASM (`^` is a power, right-associative and binding
+tighter than unary minus: -2^2 = -4); the reference pastes them into generated Python source, where `^`
+is an integer XOR.
 """
 import math
 import re

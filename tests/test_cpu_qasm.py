@@ -56,6 +56,27 @@ def test_standard_one_qubit_matrices():
                            [np.exp(1.1j) * math.sin(0.2), np.exp(0.4j) * math.cos(0.2)]])
 
 
+def test_u_gates_differ_from_the_reference_translation_by_a_global_phase():
+    """The reference translates U / u3 / u2 to qgate's U3 / U2 (the oracle's
+    'U' / 'U2' matrices, pinned to matrices recorded from the reference),
+    which carry an extra global phase exp(-i (phi + lambda) / 2)."""
+    for t, p, l in ((0.4, 1.1, -0.7), (2.9, -0.3, 1.6), (-1.2, 0.0, 2.2)):
+        want = np.asarray(sv.gate_matrix('U', (t, p, l)))
+        phase = np.exp(-0.5j * (p + l))
+        assert np.allclose(want, phase * one('U(%r, %r, %r)' % (t, p, l)), atol=1e-14)
+        assert np.allclose(want, phase * one('u3(%r, %r, %r)' % (t, p, l)), atol=1e-14)
+        assert np.allclose(np.asarray(sv.gate_matrix('U2', (p, l))),
+                           phase * one('u2(%r, %r)' % (p, l)), atol=1e-14)
+
+
+def test_expression_power_rules():
+    # '^' is a power, right-associative, binding tighter than unary minus
+    assert np.allclose(one('u1(-2^2)'), np.diag([1, np.exp(-4j)]))
+    assert np.allclose(one('u1(2^3^2 / 256)'), np.diag([1, np.exp(2j)]))
+    assert np.allclose(one('u1((-2)^2)'), np.diag([1, np.exp(4j)]))
+    assert np.allclose(one('u1(2 * 3^2 - 1)'), np.diag([1, np.exp(17j)]))
+
+
 def test_parse_registers_broadcast_user_gates_expressions():
     src = """
     OPENQASM 2.0;
