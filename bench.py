@@ -231,7 +231,39 @@ def cpu_port_gate_rate(n, ops, cs, budget_s):
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    return nbytes / dt / 1e9, done, dt, cpu_port.num_threads()
+    return nbytes / dt / 1e9, done, dt, cpu_port.num_threads(), st
+
+
+def cpu_port_observations(st, samples):
+    """Times the oracle's C port of the reference CPU runtime's observations
+    on a host state, the classes `observation_kernels` times on the GPU: Pr
+    of the highest lane (qgate/simulator/src/CPUQubitProcessor.cpp:75-125),
+    the full probability vector (FP64 here; the reference's is in the
+    state's precision), the sampling pool's normalised prefix sums
+    (CPUSamplingPool.cpp:8-63, in place) and `samples` draws from
+    default_rng(12) (CPUSamplingPool.cpp:71-81)."""
+    from oracle import cpu_port
+    n, amp = st.n, st.psi.itemsize
+    N = 1 << n
+    t0 = time.perf_counter()
+    st.calc_probability(n - 1)
+    t_prob = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    probs = st.probabilities()
+    t_vec = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    cdf, _ = cpu_port.prefix_cdf(probs, copy=False)
+    t_pool = time.perf_counter() - t0
+    u = np.random.default_rng(12).random(samples)
+    t0 = time.perf_counter()
+    cpu_port.sample_cdf(cdf, u)
+    t_samp = time.perf_counter() - t0
+    del probs, cdf
+    return {'prob': {'ms': t_prob * 1e3, 'gbs': N // 2 * amp / t_prob / 1e9},
+            'probability_vector': {'ms': t_vec * 1e3, 'gbs': (N * amp + N * 8) / t_vec / 1e9},
+            'pool_prefix_sums': {'ms': t_pool * 1e3, 'gbs': 2 * N * 8 / t_pool / 1e9},
+            'sample': {'samples': samples, 'ms': t_samp * 1e3, 'samples_per_s': samples / t_samp},
+            'threads': cpu_port.num_threads()}
 
 
 def run_reference(args):
@@ -254,6 +286,7 @@ def run_reference(args):
             st.apply(m, t, c)
     dt = time.perf_counter() - t0
     value = step_bytes * args.steps / dt / 1e9
+    observations = cpu_port_observations(st, args.samples)  # after the timed steps
     n_cx = sum(1 for _, _, _, c in sample if c)
     sample_desc = ('first %d gates of the circuit (%d U3 + %d CX) per step on a 2^%d %s state '
                    'in host memory; the port runs at the reference CPU runtime\'s own rate '
@@ -267,7 +300,8 @@ def run_reference(args):
         'config': config_block(args),
         'cpu_baseline': {'value': value, 'unit': 'GB/s', 'cores': cpu_port.num_threads(),
                          'cpu_model': cpu_model(),
-                         'kind': 'port', 'sample': sample_desc},
+                         'kind': 'port', 'sample': sample_desc,
+                         'observations': observations},
         'e2e': {'value': value, 'unit': 'GB/s', 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': 0},
     }
@@ -424,10 +458,12 @@ def run_gb300(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        gbs, done, dt, thr = cpu_port_gate_rate(n, ops, cs, args.cpu_seconds)
+        gbs, done, dt, thr, st = cpu_port_gate_rate(n, ops, cs, args.cpu_seconds)
         cpu = {'value': gbs, 'unit': 'GB/s', 'cores': thr, 'kind': 'port', 'cpu_model': cpu_model(),
                'sample': 'first %d gates of the circuit on a 2^%d %s state in host memory, '
-                         '%.1f s' % (done, n, args.dtype, dt)}
+                         '%.1f s' % (done, n, args.dtype, dt),
+               'observations': cpu_port_observations(st, args.samples)}
+        del st
 
     if rank == 0:
         per_step_passes = stats['passes'] / args.steps

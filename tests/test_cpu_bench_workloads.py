@@ -55,7 +55,7 @@ def test_reference_arm_line_carries_the_shared_config(capsys):
     import argparse
     import json
     args = argparse.Namespace(qubits=12, depth=20, dtype='c64', steps=1, warmup=0, gpus=1,
-                              ref_gates=45)
+                              ref_gates=45, samples=1000)
     bench.run_reference(args)
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line['impl'] == 'reference'
@@ -63,3 +63,6 @@ def test_reference_arm_line_carries_the_shared_config(capsys):
     assert line['metric'] == bench.METRIC and line['value'] > 0
     assert line['e2e']['h2d_bytes_per_step'] == 0 and line['e2e']['d2h_bytes_per_step'] == 0
     assert line['cpu_baseline']['kind'] == 'port' and line['cpu_baseline']['cores'] >= 1
+    obs = line['cpu_baseline']['observations']
+    assert obs['sample']['samples'] == 1000 and obs['sample']['samples_per_s'] > 0
+    assert all(obs[k]['gbs'] > 0 for k in ('prob', 'probability_vector', 'pool_prefix_sums'))
