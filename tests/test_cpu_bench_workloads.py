@@ -66,3 +66,13 @@ def test_reference_arm_line_carries_the_shared_config(capsys):
     obs = line['cpu_baseline']['observations']
     assert obs['sample']['samples'] == 1000 and obs['sample']['samples_per_s'] > 0
     assert all(obs[k]['gbs'] > 0 for k in ('prob', 'probability_vector', 'pool_prefix_sums'))
+
+
+def test_cpu_leg_helpers():
+    """The GPU arm's cpu_baseline leg: the port's gate rate on the circuit's
+    first gates and its observation timings on the same host state."""
+    ops = bench.circuit(14, 20)
+    gbs, done, dt, threads, st = bench.cpu_port_gate_rate(14, ops, 8, 0.05)
+    assert gbs > 0 and 1 <= done <= len(ops) and threads >= 1 and st.n == 14
+    obs = bench.cpu_port_observations(st, 5000)
+    assert obs['sample']['samples'] == 5000 and obs['threads'] == threads
