@@ -289,9 +289,10 @@ def run_reference(args):
     observations = cpu_port_observations(st, args.samples)  # after the timed steps
     n_cx = sum(1 for _, _, _, c in sample if c)
     sample_desc = ('first %d gates of the circuit (%d U3 + %d CX) per step on a 2^%d %s state '
-                   'in host memory; the port runs at the reference CPU runtime\'s own rate '
-                   '(oracle/port_speed.py on two x86 build hosts: port/reference 0.92-0.99x '
-                   'with 8 threads, 0.96-1.33x on one thread)' % (len(sample), len(sample) - n_cx, n_cx, n, args.dtype))
+                   'in host memory; the port runs at about the reference CPU runtime\'s own '
+                   'rate (oracle/port_speed.py on two x86 build hosts: port/reference '
+                   '0.92-0.99x with 8 threads, 0.96-1.33x on one thread)'
+                   % (len(sample), len(sample) - n_cx, n_cx, n, args.dtype))
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'GB/s',
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
