@@ -12,7 +12,7 @@ port's figure can be read as the reference's.
 The gates are the first layer of the benchmark circuit (U3 on every qubit,
 then CX on a seeded random matching), complex64; each gate counts the bytes
 of its standalone read+write sweep.  The reference applies them through its
-processor API (qgate/simulator/native_qubit_processor.py:50-63, into
+processor API (qgate/simulator/native_qubit_processor.py:50-59, into
 CPUQubitProcessor.cpp:307-362) with its own thread pool
 (qgate/simulator/src/Parallel.cpp:21-40, QGATE_NUM_WORKERS)."""
 import argparse
