@@ -860,10 +860,10 @@ static void merge_runs(std::vector<PendingGate> &gates) {
             out[prev].diag = is_diag(prod);
             continue;
         }
-        out.push_back(g);
-        int idx = (int)out.size() - 1;
+        const int idx = (int)out.size();
         last[g.target] = idx;
         for (int c : g.controls) last[c] = idx;
+        out.push_back(std::move(g));  // (`gates` is replaced by `out` below)
     }
     gates.swap(out);
 }
@@ -2182,36 +2182,58 @@ int qg_get_stream(uint64_t *stream) {
 static std::vector<std::pair<unsigned long long, std::vector<const PendingGate *>>>
 plan_gate_stages(const std::vector<PendingGate> &gates, int n, int M, int low) {
     std::vector<std::pair<unsigned long long, std::vector<const PendingGate *>>> out;
-    std::vector<const PendingGate *> remaining;
-    for (auto &g : gates) remaining.push_back(&g);
+    // (gate index, lane mask) of the gates not yet in a stage, in order
+    std::vector<std::pair<int, unsigned long long>> remaining, deferred;
+    remaining.reserve(gates.size());
+    for (size_t i = 0; i < gates.size(); ++i) remaining.emplace_back((int)i, gate_qmask(gates[i]));
     const unsigned long long all = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
     if (n <= M) M = n;
     const unsigned long long base = (n <= M) ? all : ((1ULL << low) - 1);
     while (!remaining.empty()) {
         unsigned long long S = base, blocked = 0;
-        std::vector<const PendingGate *> chosen, deferred;
-        for (auto *g : remaining) {
-            unsigned long long q = gate_qmask(*g);
+        std::vector<const PendingGate *> chosen;
+        deferred.clear();
+        for (const auto &gq : remaining) {
+            const unsigned long long q = gq.second;
             if ((q & blocked) || (int)chosen.size() >= kMaxStageGates ||
                 __builtin_popcountll(S | q) > M) {
-                deferred.push_back(g);
+                deferred.push_back(gq);
                 blocked |= q;
                 continue;
             }
             S |= q;
-            chosen.push_back(g);
+            chosen.push_back(&gates[gq.first]);
         }
         if (chosen.empty()) fail(QG_ERR_VALUE, "gate wider than a tile.");
         for (int q = 0; q < n && __builtin_popcountll(S) < M; ++q) S |= 1ULL << q;
-        out.emplace_back(S, chosen);
+        out.emplace_back(S, std::move(chosen));
         remaining.swap(deferred);
     }
     return out;
 }
 
+// Slot tables of a batch's register sets.  make_set_slots is a pure
+// function of (lanes, rl, m) and a batch reuses few distinct sets, so each
+// thread keeps the tables it has made (keyed by the lanes, 4 bits each).
 static void append_sets(const std::vector<std::vector<int>> &sets, int m, int rl,
                         std::vector<SetSlots> &sets_all) {
-    for (auto &st : sets) sets_all.push_back(make_set_slots(st.data(), rl, m, kFP32));
+    static thread_local std::unordered_map<unsigned long long, SetSlots> memo;
+    if (memo.size() > (1u << 16)) memo.clear();
+    for (auto &st : sets) {
+        unsigned long long key = ((unsigned long long)m << 32) | ((unsigned long long)rl << 28);
+        bool keyed = rl <= 7 && (int)st.size() >= rl;
+        for (int k = 0; keyed && k < rl; ++k) {
+            keyed = st[k] >= 0 && st[k] < 16;
+            key |= (unsigned long long)(st[k] & 15) << (4 * k);
+        }
+        if (!keyed) {
+            sets_all.push_back(make_set_slots(st.data(), rl, m, kFP32));
+            continue;
+        }
+        auto it = memo.find(key);
+        if (it == memo.end()) it = memo.emplace(key, make_set_slots(st.data(), rl, m, kFP32)).first;
+        sets_all.push_back(it->second);
+    }
 }
 
 // k with a 0 bit inserted at each of pos[0..npos) in turn (the host copy of
@@ -2239,38 +2261,40 @@ static unsigned host_deposit(unsigned k, unsigned mask) {
 // count of every large circuit): one wait and one completion count per item.
 constexpr int kBatchTilesPerItem = 8;
 
-int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
-                   const qg_circuit_op *gates, double *out) {
-    QG_BEGIN
-    if (prec != kFP32) fail(QG_ERR_VALUE, "batched circuits run in complex64.");
-    if (n_circuits < 1) fail(QG_ERR_VALUE, "no circuits.");
-    Device &d = dev();
-    // Plan every circuit independently (in parallel), then concatenate.
-    struct StagePart {
-        BatchStage hdr;  // ops_off / sets_off local to the circuit
-        // Tile-index bits that can be 1 in a tile with a nonzero amplitude:
-        // the run starts from |0...0>, so before this stage every amplitude
-        // whose lanes outside the earlier stages' tiles are not all 0 is
-        // still 0 (a stage mixes amplitudes only within its tiles).
-        unsigned live;
-    };
-    struct Plan {
-        int n = 0, rl = 0;
-        bool resident = false;
-        std::vector<RegOp<float>> ops;
-        std::vector<SetSlots> sets;
-        std::vector<StagePart> stages;
-        std::string error;
-    };
-    std::vector<Plan> plans(n_circuits);
+struct BatchStagePart {
+    BatchStage hdr;  // ops_off / sets_off local to the circuit
+    // Tile-index bits that can be 1 in a tile with a nonzero amplitude:
+    // the run starts from |0...0>, so before this stage every amplitude
+    // whose lanes outside the earlier stages' tiles are not all 0 is
+    // still 0 (a stage mixes amplitudes only within its tiles).
+    unsigned live;
+};
+struct BatchPlan {
+    int n = 0, rl = 0;
+    bool resident = false;
+    std::vector<RegOp<float>> ops;
+    std::vector<SetSlots> sets;
+    std::vector<BatchStagePart> stages;
+    std::string error;
+};
+
+// Plans every circuit of a batch independently (in parallel): circuits of
+// at most `resident_max` qubits as one register program over the whole
+// state, larger ones as 12-lane stages with their tile headers; a planning
+// error is recorded in the circuit's plan.
+static void plan_batch(int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
+                       const qg_circuit_op *gates, int resident_max,
+                       std::vector<BatchPlan> &plans) {
+    plans.assign(n_circuits, BatchPlan());
 #pragma omp parallel for schedule(dynamic, 8)
     for (int c = 0; c < n_circuits; ++c) {
-        Plan &P = plans[c];
+        BatchPlan &P = plans[c];
         try {
             const int n = n_qubits[c];
             P.n = n;
             if (n < 8 || n > 30) fail(QG_ERR_VALUE, "circuit %d: 8..30 qubits supported.", c);
             std::vector<PendingGate> gl;
+            gl.reserve((size_t)(gate_offsets[c + 1] - gate_offsets[c]));
             for (int64_t gi = gate_offsets[c]; gi < gate_offsets[c + 1]; ++gi) {
                 const qg_circuit_op &op = gates[gi];
                 if (op.kind != 0) fail(QG_ERR_VALUE, "circuit %d: fixed gates only.", c);
@@ -2288,12 +2312,12 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                 }
                 memcpy(g.m.v, op.mat, sizeof(g.m.v));
                 g.diag = is_diag(g.m);
-                gl.push_back(g);
+                gl.push_back(std::move(g));
             }
             merge_runs(gl);
             std::vector<RegOp<float>> prog;
             std::vector<std::vector<int>> sets;
-            if (n <= (g_dev.batch_one_launch ? 12 : 13)) {
+            if (n <= resident_max) {
                 P.resident = true;
                 P.rl = n <= 9 ? 3 : (n <= 12 ? 4 : 5);
                 std::vector<const PendingGate *> ptrs;
@@ -2301,7 +2325,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                 TileLanes tl = tile_lanes_of((1ULL << n) - 1, n);
                 build_program<float>(ptrs, tl, P.rl, prog, sets);
                 if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: program too long.", c);
-                P.ops = prog;
+                P.ops.swap(prog);
                 append_sets(sets, n, P.rl, P.sets);
             } else {
                 P.rl = 4;
@@ -2314,7 +2338,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
                     TileLanes tl = tile_lanes_of(plan[r].first, n);
                     build_program<float>(plan[r].second, tl, 4, prog, sets);
                     if (sets.size() > 255) fail(QG_ERR_RUNTIME, "circuit %d: stage too long.", c);
-                    StagePart sp;
+                    BatchStagePart sp;
                     memset(&sp.hdr, 0, sizeof(sp.hdr));
                     sp.hdr.n = n;
                     sp.hdr.m = 12;
@@ -2341,6 +2365,17 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
             P.error = "planning failed";
         }
     }
+}
+
+int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t *gate_offsets,
+                   const qg_circuit_op *gates, double *out) {
+    QG_BEGIN
+    if (prec != kFP32) fail(QG_ERR_VALUE, "batched circuits run in complex64.");
+    if (n_circuits < 1) fail(QG_ERR_VALUE, "no circuits.");
+    Device &d = dev();
+    // Plan every circuit independently (in parallel), then concatenate.
+    std::vector<BatchPlan> plans;
+    plan_batch(n_circuits, n_qubits, gate_offsets, gates, d.batch_one_launch ? 12 : 13, plans);
     for (auto &P : plans)
         if (!P.error.empty()) fail(QG_ERR_VALUE, "%s", P.error.c_str());
 
@@ -2381,7 +2416,7 @@ int qg_batch_sum_z(int prec, int n_circuits, const int *n_qubits, const int64_t 
     std::vector<int> big_n, big_idx;
     long long arena_elems = 0;
     for (int c = 0; c < n_circuits; ++c) {
-        Plan &P = plans[c];
+        BatchPlan &P = plans[c];
         const long long ops_base = ops_at[c];
         const int sets_base = (int)sets_at[c];
         if (P.resident) {
